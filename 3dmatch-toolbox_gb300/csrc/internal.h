@@ -1,0 +1,66 @@
+// Launchers shared between translation units of libtdm (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "tdm.h"
+
+namespace tdm {
+
+// ---- conv_simt.cu ----
+tdm_status launch_conv1(const float* patches, int B, const float* w, const float* bias, bool bf16_out, void* out,
+                        int64_t out_cs, cudaStream_t s);
+tdm_status launch_conv_f32(const float* in, int B, int D, int C, int ks, const float* w, const float* bias, int K,
+                           bool relu, float* out, cudaStream_t s);
+tdm_status launch_pool_f32(const float* in, int B, int D, int C, float* out, cudaStream_t s);
+tdm_status launch_pool_c8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out, int64_t out_cs,
+                          cudaStream_t s);
+
+// ---- conv_tc.cu: tcgen05 implicit-GEMM convolution / GEMM ----
+// Output layouts of the tensor-core epilogue.
+enum TcOutMode : int {
+  TC_OUT_C8_CONV = 0,   // chunk-planar, re-linearised from the D^3 input grid to the Do^3 output grid
+  TC_OUT_C8_TAPS = 1,   // chunk-planar GEMM operand: K index = tap*Cout + c, row = patch (conv7 -> conv8)
+  TC_OUT_C8_ROWS = 2,   // chunk-planar, row = input row (GEMM outputs)
+  TC_OUT_F32_ROWS = 3,  // float [rows][Cout]
+};
+
+struct TcLayer {
+  // geometry
+  int cin, cout;
+  int D, Do;      // input / output spatial extent (conv); D = 1 for a GEMM
+  int nz, nyx;    // tap structure: (3, 9) for 3x3x3 conv, (1, 1) for a GEMM
+  int kgroups;    // 128-byte K groups per tap (cin*elem/128)
+  int nt, msub;   // N tile and number of 128-row M sub-tiles per CTA
+  int out_mode;
+  int relu;
+  bool fp8_in;    // operands are E4M3 (kind::f8f6f4)
+  bool fp8_out;   // epilogue writes E4M3 (chunk of 16 channels per 16 bytes)
+  // device data
+  uint8_t* wpk;   // packed weights, blocks [ntile][zt][cg][yx] of nt*128 bytes
+  float* bias;    // [cout]
+  float* wscale;  // per-output-channel dequantisation scale (FP8) or null
+};
+
+struct TcArgs {
+  const uint8_t* act;
+  int64_t act_cs;  // bytes between input chunks
+  int64_t rows;    // input rows (B*D^3 conv; B GEMM)
+  uint8_t* out;
+  int64_t out_cs;  // bytes between output chunks
+  float in_scale;  // FP8: activation dequantisation scale of the input
+  float out_qinv;  // FP8 output: 1/scale used to quantise
+};
+
+// Rows of slack a chunk-planar input needs after its last row for layer L.
+int64_t tc_tail_rows(const TcLayer& L);
+tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s);
+// Packs Marvin-layout weights [cout][cin][taps] (taps = nz*nyx, or the GEMM
+// K flattening for conv8) into the tcgen05 block layout; returns host bytes.
+void pack_tc_weights(const TcLayer& L, const float* w, int gemm_taps, std::vector<uint8_t>* out,
+                     std::vector<float>* scales);
+
+}  // namespace tdm

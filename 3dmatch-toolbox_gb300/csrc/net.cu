@@ -1,0 +1,426 @@
+// The 3DMatch descriptor net (core/3dmatch-net-test.json): conv1..conv8 3x3x3
+// valid convolutions with ReLU, 2^3 max-pool after conv2, then `feat`, a
+// 1x1x1 512->512 convolution without ReLU.  30^3 TDF patch -> 512-d.
+//
+// Replaces marvin::Net as demo.cu drives it (core/demo.cu:179-231): weights
+// are found by layer name in a .marvin file (Layer::setWeights,
+// core/marvin.hpp:3321-3370), buffers are owned by the handle, and forward
+// runs the layer sequence.  Precisions:
+//   FP32: CUDA-core implicit GEMM for every layer (the drop-in form).
+//   BF16: conv1 on CUDA cores (K = 27), conv2..feat on tcgen05 with BF16
+//         operands, FP32 accumulation, BF16 activations between layers.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+#include "marvin_io.h"
+
+using namespace tdm;
+
+namespace {
+const char* kNames[9] = {"conv1", "conv2", "conv3", "conv4", "conv5", "conv6", "conv7", "conv8", "feat"};
+const int kCout[9] = {64, 64, 128, 128, 256, 256, 512, 512, 512};
+const int kCin[9] = {1, 64, 64, 128, 128, 256, 256, 512, 512};
+const int kKs[9] = {3, 3, 3, 3, 3, 3, 3, 3, 1};
+const int kDin[9] = {30, 28, 13, 11, 9, 7, 5, 3, 1};  // input extent of each layer (pool after conv2)
+constexpr int kDefaultMaxBatch = 2048;
+// Response ids: layer index 0..8 (conv1..conv8, feat) = that layer's output
+// (after its in-place ReLU); kPool = pool1.  -1 = the full forward.
+constexpr int kPool = 100;
+
+// Chunk-planar BF16 -> channels-last float (responses of the BF16 form).
+// taps_layout: rows are patches and chunk = tap*(C/8) + c/8 (conv7's output).
+__global__ void c8_to_f32_kernel(const uint8_t* __restrict__ in, int64_t cs, int64_t npos, int C, int taps_layout,
+                                 int ntaps, float* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npos * C) return;
+  int c = (int)(i % C);
+  int64_t p = i / C;
+  int64_t chunk, row;
+  if (taps_layout) {
+    int64_t b = p / ntaps;
+    int t = (int)(p - b * ntaps);
+    chunk = (int64_t)t * (C / 8) + c / 8;
+    row = b;
+  } else {
+    chunk = c / 8;
+    row = p;
+  }
+  __nv_bfloat16 v = *reinterpret_cast<const __nv_bfloat16*>(in + chunk * cs + row * 16 + (c % 8) * 2);
+  out[i] = __bfloat162float(v);
+}
+}  // namespace
+
+struct tdm_net {
+  tdm_precision prec = TDM_FP32;
+  int use_feat = 1;
+  int device = 0;
+  std::vector<float> hw[9], hb[9];  // Marvin layout: [K][C][taps], [K]
+  float* d_b[9] = {};
+  float* d_w1 = nullptr;  // conv1 [27][64]
+  float* d_w32[9] = {};   // FP32 path: [taps*C][K]
+  TcLayer tc[9];          // tcgen05 layers (index 1..8)
+  std::vector<void*> allocs;
+  uint8_t* ws = nullptr;
+  size_t ws_bytes = 0;
+  int max_batch = kDefaultMaxBatch;
+
+  ~tdm_net() {
+    for (void* p : allocs) cudaFree(p);
+    if (ws) cudaFree(ws);
+  }
+  template <typename T>
+  tdm_status upload(const T* h, size_t n, T** d) {
+    void* p = nullptr;
+    TDM_CHECK_CUDA(cudaMalloc(&p, n * sizeof(T)));
+    allocs.push_back(p);
+    TDM_CHECK_CUDA(cudaMemcpy(p, h, n * sizeof(T), cudaMemcpyHostToDevice));
+    *d = static_cast<T*>(p);
+    return TDM_OK;
+  }
+};
+
+namespace {
+
+int64_t round16(int64_t x) { return (x + 15) & ~(int64_t)15; }
+
+TcLayer make_tc_layer(int l, bool use_feat) {
+  TcLayer L{};
+  L.cin = kCin[l];
+  L.cout = kCout[l];
+  L.relu = l < 8 ? 1 : 0;
+  L.fp8_in = L.fp8_out = false;
+  if (l <= 6) {  // 3x3x3 conv on a grid
+    L.D = kDin[l];
+    L.Do = L.D - 2;
+    L.nz = 3;
+    L.nyx = 9;
+    L.kgroups = L.cin / 64;
+    L.out_mode = l == 6 ? TC_OUT_C8_TAPS : TC_OUT_C8_CONV;
+  } else {  // conv8 (K = 27*512, flattened) and feat (K = 512) as GEMMs over patches
+    L.D = 1;
+    L.Do = 1;
+    L.nz = 1;
+    L.nyx = 1;
+    L.kgroups = (l == 7 ? 27 * 512 : 512) / 64;
+    L.out_mode = (l == 7 && use_feat) ? TC_OUT_C8_ROWS : TC_OUT_F32_ROWS;
+  }
+  if (L.cout == 64) { L.nt = 64; L.msub = 4; }
+  else if (L.cout == 128) { L.nt = 128; L.msub = 4; }
+  else { L.nt = 256; L.msub = 2; }
+  return L;
+}
+
+tdm_status setup_weights(tdm_net* net) {
+  // biases and conv1 (all precisions)
+  for (int l = 0; l < 9; ++l) {
+    tdm_status st = net->upload(net->hb[l].data(), net->hb[l].size(), &net->d_b[l]);
+    if (st != TDM_OK) return st;
+  }
+  std::vector<float> w1(27 * 64);
+  for (int k = 0; k < 64; ++k)
+    for (int t = 0; t < 27; ++t) w1[t * 64 + k] = net->hw[0][k * 27 + t];
+  tdm_status st = net->upload(w1.data(), w1.size(), &net->d_w1);
+  if (st != TDM_OK) return st;
+  if (net->prec == TDM_FP32) {
+    for (int l = 1; l < 9; ++l) {
+      int K = kCout[l], C = kCin[l], T = kKs[l] * kKs[l] * kKs[l];
+      std::vector<float> wt((size_t)T * C * K);
+      for (int k = 0; k < K; ++k)
+        for (int c = 0; c < C; ++c)
+          for (int t = 0; t < T; ++t) wt[((size_t)t * C + c) * K + k] = net->hw[l][((size_t)k * C + c) * T + t];
+      st = net->upload(wt.data(), wt.size(), &net->d_w32[l]);
+      if (st != TDM_OK) return st;
+    }
+    return TDM_OK;
+  }
+  if (net->prec == TDM_BF16) {
+    for (int l = 1; l < 9; ++l) {
+      TcLayer L = make_tc_layer(l, net->use_feat != 0);
+      std::vector<uint8_t> pk;
+      std::vector<float> sc;
+      pack_tc_weights(L, net->hw[l].data(), l == 7 ? 27 : 1, &pk, &sc);
+      st = net->upload(pk.data(), pk.size(), &L.wpk);
+      if (st != TDM_OK) return st;
+      L.bias = net->d_b[l];
+      L.wscale = nullptr;
+      net->tc[l] = L;
+    }
+    return TDM_OK;
+  }
+  return fail(TDM_ERR_UNSUPPORTED, "precision not available for the net yet");
+}
+
+tdm_status create_common(tdm_net* net, tdm_precision prec, int32_t use_feat) {
+  net->prec = prec;
+  net->use_feat = use_feat ? 1 : 0;
+  TDM_CHECK_CUDA(cudaGetDevice(&net->device));
+  return setup_weights(net);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 forward of one chunk: buffers hold channels-last float activations.
+// ---------------------------------------------------------------------------
+// Output extent and channels of each response.
+void response_shape(int id, int* D, int* C) {
+  static const int Dout[9] = {28, 26, 11, 9, 7, 5, 3, 1, 1};
+  if (id == kPool) { *D = 13; *C = 64; return; }
+  *D = Dout[id];
+  *C = kCout[id];
+}
+
+tdm_status copy_response_f32(const float* src, int B, int id, float* out, cudaStream_t s) {
+  int D, C;
+  response_shape(id, &D, &C);
+  TDM_CHECK_CUDA(cudaMemcpyAsync(out, src, sizeof(float) * (size_t)B * D * D * D * C, cudaMemcpyDeviceToDevice, s));
+  return TDM_OK;
+}
+
+tdm_status forward_f32(tdm_net* net, const float* patches, int B, float* desc, int stop, cudaStream_t s) {
+  float* b0 = reinterpret_cast<float*>(net->ws);
+  float* b1 = b0 + (size_t)B * 1404928;  // 28^3 * 64
+  tdm_status st = launch_conv1(patches, B, net->d_w1, net->d_b[0], false, b0, 0, s);
+  if (st) return st;
+  if (stop == 0) return copy_response_f32(b0, B, 0, desc, s);
+  float* in = b0;
+  float* out = b1;
+  for (int l = 1; l < 9; ++l) {
+    if (l == 8 && !net->use_feat) break;
+    bool last = stop < 0 && ((l == 8) || (l == 7 && !net->use_feat));
+    float* dst = last ? desc : out;
+    st = launch_conv_f32(in, B, kDin[l], kCin[l], kKs[l], net->d_w32[l], net->d_b[l], kCout[l], l < 8, dst, s);
+    if (st) return st;
+    if (stop == l) return copy_response_f32(dst, B, l, desc, s);
+    if (l == 1) {  // 2^3 max-pool after conv2 (26^3 -> 13^3)
+      st = launch_pool_f32(dst, B, 26, 64, in, s);
+      if (st) return st;
+      if (stop == kPool) return copy_response_f32(in, B, kPool, desc, s);
+      continue;  // pooled result is back in `in`
+    }
+    std::swap(in, out);
+  }
+  return TDM_OK;
+}
+
+size_t f32_ws_bytes(int B) { return (size_t)B * (1404928 + 1124864) * sizeof(float); }
+
+// ---------------------------------------------------------------------------
+// BF16 forward of one chunk (chunk-planar BF16 activations).
+// ---------------------------------------------------------------------------
+struct Bf16Plan {
+  int64_t rows_alloc[9];  // rows allocated per chunk for the input of layer l
+  int64_t rows[9];        // live rows of the input of layer l
+  size_t off1;            // byte offset of buffer 1
+  size_t total;
+};
+
+Bf16Plan bf16_plan(const tdm_net* net, int B) {
+  Bf16Plan P{};
+  // inputs: l=1 conv2 (28^3), pool input (26^3) handled separately, l=2 conv3 (13^3) ...
+  for (int l = 1; l < 9; ++l) {
+    int64_t rows = l <= 6 ? (int64_t)B * kDin[l] * kDin[l] * kDin[l] : B;
+    P.rows[l] = rows;
+    P.rows_alloc[l] = rows + tc_tail_rows(net->tc[l]);
+  }
+  // buffer 0 holds inputs of l = 1, 2(pooled), 4, 6, 8; buffer 1: conv2 output (pool input), 3, 5, 7
+  auto chunks = [](int l) { return kCin[l] / 8; };
+  size_t b0 = 0, b1 = 0;
+  for (int l : {1, 2, 4, 6, 8}) b0 = std::max(b0, (size_t)(l == 7 ? 1728 : chunks(l)) * P.rows_alloc[l] * 16);
+  b1 = std::max(b1, (size_t)8 * ((int64_t)B * 17576 + 8) * 16);  // conv2 output (pre-pool)
+  for (int l : {3, 5}) b1 = std::max(b1, (size_t)chunks(l) * P.rows_alloc[l] * 16);
+  b1 = std::max(b1, (size_t)1728 * P.rows_alloc[7] * 16);  // conv7 -> conv8 flattened operand
+  P.off1 = round16((int64_t)b0) + 4096;
+  P.total = P.off1 + b1 + 4096;
+  return P;
+}
+
+tdm_status c8_response(const uint8_t* src, int64_t cs, int B, int id, bool taps, float* out, cudaStream_t s) {
+  int D, C;
+  response_shape(id, &D, &C);
+  int64_t npos = (int64_t)B * D * D * D;
+  c8_to_f32_kernel<<<(unsigned)((npos * C + 255) / 256), 256, 0, s>>>(src, cs, npos, C, taps ? 1 : 0, D * D * D, out);
+  TDM_CHECK_LAUNCH("c8_to_f32_kernel");
+  return TDM_OK;
+}
+
+tdm_status forward_bf16(tdm_net* net, const float* patches, int B, float* desc, int stop, cudaStream_t s) {
+  Bf16Plan P = bf16_plan(net, B);
+  uint8_t* b0 = net->ws;
+  uint8_t* b1 = net->ws + P.off1;
+  // conv1 -> chunk-planar BF16 input of conv2
+  int64_t cs = P.rows_alloc[1] * 16;
+  tdm_status st = launch_conv1(patches, B, net->d_w1, net->d_b[0], true, b0, cs, s);
+  if (st) return st;
+  if (stop == 0) return c8_response(b0, cs, B, 0, false, desc, s);
+  uint8_t* cur = b0;
+  int64_t cur_cs = cs;
+  for (int l = 1; l < 9; ++l) {
+    if (l == 8 && !net->use_feat) break;
+    const TcLayer& L = net->tc[l];
+    bool last = (l == 8) || (l == 7 && !net->use_feat);
+    uint8_t* dst = (cur == b0) ? b1 : b0;
+    TcArgs a{};
+    a.act = cur;
+    a.act_cs = cur_cs;
+    a.rows = P.rows[l];
+    a.in_scale = 1.0f;
+    a.out_qinv = 1.0f;
+    int64_t out_cs = 0;
+    if (last) {
+      a.out = reinterpret_cast<uint8_t*>(desc);
+      a.out_cs = 0;
+    } else if (l == 1) {
+      out_cs = ((int64_t)B * 17576 + 8) * 16;  // conv2 output, read by the pool
+      a.out = dst;
+      a.out_cs = out_cs;
+    } else {
+      out_cs = P.rows_alloc[l + 1] * 16;
+      a.out = dst;
+      a.out_cs = out_cs;
+    }
+    st = launch_tc_layer(L, a, s);
+    if (st) return st;
+    if (last) break;
+    if (stop == l) return c8_response(dst, out_cs, B, l, L.out_mode == TC_OUT_C8_TAPS, desc, s);
+    if (l == 1) {  // pool 26^3 -> 13^3 back into buffer 0 as conv3's input
+      int64_t pcs = P.rows_alloc[2] * 16;
+      st = launch_pool_c8(dst, out_cs, B, 26, 8, cur, pcs, s);
+      if (st) return st;
+      if (stop == kPool) return c8_response(cur, pcs, B, kPool, false, desc, s);
+      cur_cs = pcs;
+      continue;
+    }
+    cur = dst;
+    cur_cs = out_cs;
+  }
+  return TDM_OK;
+}
+
+tdm_status ensure_ws(tdm_net* net, size_t bytes) {
+  if (net->ws_bytes >= bytes) return TDM_OK;
+  if (net->ws) {
+    TDM_CHECK_CUDA(cudaDeviceSynchronize());
+    cudaFree(net->ws);
+    net->ws = nullptr;
+    net->ws_bytes = 0;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) return cuda_status(e, "net workspace");
+  TDM_CHECK_CUDA(cudaMemset(p, 0, bytes));
+  net->ws = static_cast<uint8_t*>(p);
+  net->ws_bytes = bytes;
+  return TDM_OK;
+}
+
+tdm_status load_host_weights(tdm_net* net, const float* const* w, const float* const* b) {
+  for (int l = 0; l < 9; ++l) {
+    size_t n = (size_t)kCout[l] * kCin[l] * kKs[l] * kKs[l] * kKs[l];
+    if (!w[l] || !b[l]) return fail(TDM_ERR_INVALID_ARG, std::string("missing weights for ") + kNames[l]);
+    net->hw[l].assign(w[l], w[l] + n);
+    net->hb[l].assign(b[l], b[l] + kCout[l]);
+  }
+  return TDM_OK;
+}
+
+}  // namespace
+
+extern "C" tdm_status tdm_net_create_from_host(const float* const* w, const float* const* b, tdm_precision prec,
+                                               int32_t use_feat, tdm_net** out) {
+  TDM_REQUIRE(w && b && out, "tdm_net_create_from_host: null pointer");
+  TDM_REQUIRE(prec == TDM_FP32 || prec == TDM_BF16 || prec == TDM_FP8, "tdm_net_create_from_host: bad precision");
+  tdm_net* net = new tdm_net();
+  tdm_status st = load_host_weights(net, w, b);
+  if (st == TDM_OK) st = create_common(net, prec, use_feat);
+  if (st != TDM_OK) {
+    delete net;
+    return st;
+  }
+  *out = net;
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_net_create(const char* path, tdm_precision prec, int32_t use_feat, tdm_net** out) {
+  TDM_REQUIRE(path && out, "tdm_net_create: null pointer");
+  std::map<std::string, MarvinTensor> t;
+  std::string err;
+  tdm_status st = read_marvin(path, &t, &err);
+  if (st != TDM_OK) return fail(st, err);
+  const float* w[9];
+  const float* b[9];
+  for (int l = 0; l < 9; ++l) {
+    auto iw = t.find(std::string(kNames[l]) + ".weight");
+    auto ib = t.find(std::string(kNames[l]) + ".bias");
+    if (iw == t.end() || ib == t.end()) return fail(TDM_ERR_FORMAT, std::string("weight file lacks ") + kNames[l]);
+    size_t n = (size_t)kCout[l] * kCin[l] * kKs[l] * kKs[l] * kKs[l];
+    if (iw->second.data.size() != n || ib->second.data.size() != (size_t)kCout[l])
+      return fail(TDM_ERR_FORMAT, std::string("element count mismatch for ") + kNames[l]);
+    w[l] = iw->second.data.data();
+    b[l] = ib->second.data.data();
+  }
+  return tdm_net_create_from_host(w, b, prec, use_feat, out);
+}
+
+static tdm_status net_run(tdm_net* net, const float* patches, int32_t b, float* out, int stop, tdm_stream s) {
+  if (b == 0) return TDM_OK;
+  TDM_REQUIRE(patches && out, "tdm_net_forward: null pointer");
+  const int chunk = std::min<int>(b, net->max_batch);
+  size_t need = net->prec == TDM_FP32 ? f32_ws_bytes(chunk) : bf16_plan(net, chunk).total;
+  tdm_status st = ensure_ws(net, need);
+  if (st) return st;
+  size_t per = 512;
+  if (stop >= 0) {
+    int D, C;
+    response_shape(stop, &D, &C);
+    per = (size_t)D * D * D * C;
+  }
+  for (int i = 0; i < b; i += chunk) {
+    int n = std::min(chunk, b - i);
+    const float* p = patches + (size_t)i * 27000;
+    float* d = out + (size_t)i * per;
+    st = net->prec == TDM_FP32 ? forward_f32(net, p, n, d, stop, s) : forward_bf16(net, p, n, d, stop, s);
+    if (st) return st;
+  }
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_net_forward(tdm_net* net, const float* patches, int32_t b, float* desc, tdm_stream s) {
+  TDM_REQUIRE(net && b >= 0, "tdm_net_forward: bad arguments");
+  return net_run(net, patches, b, desc, -1, s);
+}
+
+extern "C" tdm_status tdm_net_response(tdm_net* net, const char* name, const float* patches, int32_t b, float* out,
+                                       tdm_stream s) {
+  TDM_REQUIRE(net && name && b >= 0, "tdm_net_response: bad arguments");
+  std::string n(name);
+  int id = -2;
+  for (int l = 0; l < 9; ++l)
+    if (n == kNames[l]) id = l;
+  if (n == "pool1") id = kPool;
+  TDM_REQUIRE(id != -2, "tdm_net_response: unknown response name");
+  TDM_REQUIRE(!(id == 8 && !net->use_feat), "tdm_net_response: net built without feat");
+  return net_run(net, patches, b, out, id, s);
+}
+
+extern "C" tdm_status tdm_net_set_max_batch(tdm_net* net, int32_t max_batch) {
+  TDM_REQUIRE(net && max_batch > 0, "tdm_net_set_max_batch: bad arguments");
+  net->max_batch = max_batch;
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_net_destroy(tdm_net* net) {
+  delete net;
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_write_seeded_weights(const char* path, uint64_t seed) {
+  TDM_REQUIRE(path, "tdm_write_seeded_weights: null path");
+  std::string err;
+  tdm_status st = write_marvin_f32(path, seeded_weights(seed), &err);
+  if (st != TDM_OK) return fail(st, err);
+  return TDM_OK;
+}

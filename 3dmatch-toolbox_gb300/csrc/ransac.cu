@@ -1,0 +1,351 @@
+// RANSAC rigid registration with Kabsch refit.
+//
+// Replaces ransacfitRt.m (core/external/sfm/ransacfitRt.m:20-38), ransac.m
+// (core/external/peter/ransac.m:113-232) and estimateRt.m.  Model x = R y + t
+// (x: fragment-1 keypoints, y: fragment-2 keypoints).  Every trial h draws 3
+// distinct correspondences from a counter-based stream (splitmix64 keyed by
+// seed and 3h+j), fits R,t with Kabsch in FP64 (covariance, SVD through the
+// Jacobi eigen-decomposition of H^T H), and counts inliers in FP32 with the
+// strict |x - (R y + t)| < threshold of euc3Ddist.  The best count wins and
+// ties go to the later trial (ransac.m:194 uses >=).  The final model is the
+// FP64 Kabsch refit on the winner's inliers (ransacfitRt.m:37).
+//
+// This translation unit is compiled with -fmad=false: the CPU oracle performs
+// the same operations in the same order, so trial counts and inlier sets are
+// identical on both.
+#include <cfloat>
+
+#include "common.cuh"
+
+namespace tdm {
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ uint32_t bounded(uint64_t seed, uint64_t ctr, uint32_t n) {
+  return (uint32_t)__umul64hi(mix64(seed + (ctr + 1) * 0x9E3779B97F4A7C15ULL), (uint64_t)n);
+}
+
+__device__ void sample3(uint64_t seed, uint32_t h, int m, int s[3]) {
+  uint32_t i0 = bounded(seed, 3ull * h + 0, (uint32_t)m);
+  uint32_t i1 = bounded(seed, 3ull * h + 1, (uint32_t)(m - 1));
+  uint32_t i2 = bounded(seed, 3ull * h + 2, (uint32_t)(m - 2));
+  if (i1 >= i0) i1++;
+  uint32_t lo = i0 < i1 ? i0 : i1, hi = i0 < i1 ? i1 : i0;
+  if (i2 >= lo) i2++;
+  if (i2 >= hi) i2++;
+  s[0] = (int)i0; s[1] = (int)i1; s[2] = (int)i2;
+}
+
+__device__ void jacobi3(double A[3][3], double V[3][3], double ev[3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 24; ++sweep) {
+    double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+    double scale = fabs(A[0][0]) + fabs(A[1][1]) + fabs(A[2][2]);
+    if (off <= 1e-300 || off <= 1e-18 * scale) break;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        double apq = A[p][q];
+        if (apq == 0.0) continue;
+        double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+        double t = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
+        if (theta < 0.0) t = -t;
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 3; ++k) {
+          double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - s * akq;
+          A[k][q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - s * aqk;
+          A[q][k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double vkp = V[k][p], vkq = V[k][q];
+          V[k][p] = c * vkp - s * vkq;
+          V[k][q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < 3; ++i) ev[i] = A[i][i];
+}
+
+// R (row-major) and t from the centred cross-covariance H = sum (y-cy)(x-cx)^T.
+__device__ bool kabsch_from_h(const double H[3][3], const double cx[3], const double cy[3], double R[9],
+                              double t[3]) {
+  double M[3][3], V[3][3], ev[3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += H[k][i] * H[k][j];
+      M[i][j] = s;
+    }
+  jacobi3(M, V, ev);
+  int o[3] = {0, 1, 2};
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2 - i; ++j)
+      if (ev[o[j]] < ev[o[j + 1]]) { int tmp = o[j]; o[j] = o[j + 1]; o[j + 1] = tmp; }
+  double v[3][3], u[3][3];
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) v[c][r] = V[r][o[c]];
+  v[2][0] = v[0][1] * v[1][2] - v[0][2] * v[1][1];
+  v[2][1] = v[0][2] * v[1][0] - v[0][0] * v[1][2];
+  v[2][2] = v[0][0] * v[1][1] - v[0][1] * v[1][0];
+  for (int c = 0; c < 2; ++c) {
+    double hv[3], n = 0.0;
+    for (int r = 0; r < 3; ++r) {
+      hv[r] = H[r][0] * v[c][0] + H[r][1] * v[c][1] + H[r][2] * v[c][2];
+      n += hv[r] * hv[r];
+    }
+    n = sqrt(n);
+    if (!(n > 1e-300)) return false;
+    for (int r = 0; r < 3; ++r) u[c][r] = hv[r] / n;
+  }
+  {
+    double d = u[0][0] * u[1][0] + u[0][1] * u[1][1] + u[0][2] * u[1][2], n = 0.0;
+    for (int r = 0; r < 3; ++r) { u[1][r] = u[1][r] - d * u[0][r]; n += u[1][r] * u[1][r]; }
+    n = sqrt(n);
+    if (!(n > 1e-300)) return false;
+    for (int r = 0; r < 3; ++r) u[1][r] = u[1][r] / n;
+  }
+  u[2][0] = u[0][1] * u[1][2] - u[0][2] * u[1][1];
+  u[2][1] = u[0][2] * u[1][0] - u[0][0] * u[1][2];
+  u[2][2] = u[0][0] * u[1][1] - u[0][1] * u[1][0];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[3 * i + j] = v[0][i] * u[0][j] + v[1][i] * u[1][j] + v[2][i] * u[2][j];
+  for (int i = 0; i < 3; ++i) t[i] = cx[i] - (R[3 * i] * cy[0] + R[3 * i + 1] * cy[1] + R[3 * i + 2] * cy[2]);
+  return true;
+}
+
+// Kabsch on the listed correspondences (idx == nullptr: 0..n-1).
+__device__ bool kabsch(const float* x, const float* y, const int* idx, int n, double R[9], double t[3]) {
+  double cx[3] = {0, 0, 0}, cy[3] = {0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    int k = idx ? idx[i] : i;
+    for (int a = 0; a < 3; ++a) { cx[a] += (double)x[3 * k + a]; cy[a] += (double)y[3 * k + a]; }
+  }
+  for (int a = 0; a < 3; ++a) { cx[a] /= (double)n; cy[a] /= (double)n; }
+  double H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int i = 0; i < n; ++i) {
+    int k = idx ? idx[i] : i;
+    double dx[3], dy[3];
+    for (int a = 0; a < 3; ++a) { dx[a] = (double)x[3 * k + a] - cx[a]; dy[a] = (double)y[3 * k + a] - cy[a]; }
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) H[a][b] += dy[a] * dx[b];
+  }
+  return kabsch_from_h(H, cx, cy, R, t);
+}
+
+__device__ __forceinline__ bool is_inlier(const float* xi, const float* yi, const float Rf[9], const float tf[3],
+                                          float thr2) {
+  float px = Rf[0] * yi[0] + Rf[1] * yi[1] + Rf[2] * yi[2] + tf[0];
+  float py = Rf[3] * yi[0] + Rf[4] * yi[1] + Rf[5] * yi[2] + tf[1];
+  float pz = Rf[6] * yi[0] + Rf[7] * yi[1] + Rf[8] * yi[2] + tf[2];
+  float ex = xi[0] - px, ey = xi[1] - py, ez = xi[2] - pz;
+  float d2 = ex * ex + ey * ey + ez * ez;
+  return d2 < thr2;
+}
+
+// Trial model for h (false when the sample is degenerate).
+__device__ bool trial_model(const float* x, const float* y, int m, uint64_t seed, uint32_t h, float Rf[9],
+                            float tf[3]) {
+  int s[3];
+  sample3(seed, h, m, s);
+  double R[9], t[3];
+  if (!kabsch(x, y, s, 3, R, t)) return false;
+  for (int i = 0; i < 9; ++i) Rf[i] = (float)R[i];
+  for (int i = 0; i < 3; ++i) tf[i] = (float)t[i];
+  return true;
+}
+
+// One thread per trial; correspondences staged in shared memory (x then y).
+__global__ __launch_bounds__(256) void trials_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                                     const int32_t* __restrict__ m_dev, int m_max, int smem_pts,
+                                                     uint64_t seed, int iters, float thr, int32_t* __restrict__ counts,
+                                                     unsigned long long* __restrict__ best) {
+  extern __shared__ float sp[];
+  int m = *m_dev;
+  m = m < m_max ? m : m_max;
+  const bool staged = m <= smem_pts;
+  if (staged) {
+    for (int i = threadIdx.x; i < 3 * m; i += blockDim.x) {
+      sp[i] = x[i];
+      sp[3 * smem_pts + i] = y[i];
+    }
+  }
+  __syncthreads();
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= iters) return;
+  int c = 0;
+  if (m >= 3) {
+    const float* xs = staged ? sp : x;
+    const float* ys = staged ? sp + 3 * smem_pts : y;
+    float Rf[9], tf[3];
+    if (trial_model(xs, ys, m, seed, (uint32_t)h, Rf, tf)) {
+      const float thr2 = thr * thr;
+      for (int i = 0; i < m; ++i) c += is_inlier(xs + 3 * i, ys + 3 * i, Rf, tf, thr2) ? 1 : 0;
+    }
+  }
+  counts[h] = c;
+  atomicMax(best, ((unsigned long long)(uint32_t)c << 32) | (unsigned long long)(uint32_t)h);
+}
+
+// Winner, ordered inlier list and FP64 refit (one block).
+__global__ __launch_bounds__(1024) void finalize_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                                        const int32_t* __restrict__ m_dev, int m_max, uint64_t seed,
+                                                        int iters, float thr, int adaptive, int max_trials,
+                                                        const int32_t* __restrict__ counts,
+                                                        const unsigned long long* __restrict__ best,
+                                                        double* __restrict__ rt, int32_t* __restrict__ inliers,
+                                                        int32_t* __restrict__ info) {
+  __shared__ int s_h, s_trials, s_ok;
+  __shared__ float sR[9], st[3];
+  __shared__ int s_warp[32];
+  __shared__ int s_base;
+  int m = *m_dev;
+  m = m < m_max ? m : m_max;
+  if (threadIdx.x == 0) {
+    int h = -1, trials = iters;
+    if (m >= 3 && iters > 0) {
+      if (adaptive) {
+        // ransac.m:139-221 loop replayed over the scored trials
+        double N = 1.0, p = 0.99, eps = 2.220446049250313e-16;
+        int bestscore = 0, tc = 0;
+        while (N > (double)tc && tc < iters) {
+          int c = counts[tc];
+          if (c >= bestscore) {
+            bestscore = c;
+            h = tc;
+            double w = (double)c / (double)m;
+            double pno = 1.0 - w * w * w;
+            if (pno < eps) pno = eps;
+            if (pno > 1.0 - eps) pno = 1.0 - eps;
+            N = log(1.0 - p) / log(pno);
+            if (N < 10.0) N = 10.0;
+          }
+          tc++;
+          if (tc > max_trials) break;
+        }
+        trials = tc;
+      } else {
+        h = (int)(uint32_t)(*best & 0xFFFFFFFFull);
+      }
+    }
+    s_h = h;
+    s_trials = trials;
+    s_ok = 0;
+    if (h >= 0 && counts[h] > 0) {
+      float Rf[9], tf[3];
+      if (trial_model(x, y, m, seed, (uint32_t)h, Rf, tf)) {
+        for (int i = 0; i < 9; ++i) sR[i] = Rf[i];
+        for (int i = 0; i < 3; ++i) st[i] = tf[i];
+        s_ok = 1;
+      }
+    }
+    s_base = 0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (s_ok) {
+    const float thr2 = thr * thr;
+    for (int i0 = 0; i0 < m; i0 += blockDim.x) {
+      int i = i0 + threadIdx.x;
+      int f = (i < m) && is_inlier(x + 3 * i, y + 3 * i, sR, st, thr2) ? 1 : 0;
+      unsigned bal = __ballot_sync(0xffffffffu, f);
+      int pre = __popc(bal & ((1u << lane) - 1));
+      if (lane == 31) s_warp[w] = pre + f;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int q = 0; q < nw; ++q) { int t = s_warp[q]; s_warp[q] = acc; acc += t; }
+        s_warp[31] = acc;
+      }
+      __syncthreads();
+      if (f) inliers[s_base + s_warp[w] + pre] = i;
+      __syncthreads();
+      if (threadIdx.x == 0) s_base += s_warp[31];
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0) {
+    int n = s_ok ? s_base : 0;
+    double R[9], t[3];
+    bool fit = n >= 3 && kabsch(x, y, inliers, n, R, t);
+    for (int i = 0; i < 3; ++i) {
+      for (int j = 0; j < 3; ++j) rt[4 * i + j] = fit ? R[3 * i + j] : (i == j ? 1.0 : 0.0);
+      rt[4 * i + 3] = fit ? t[i] : 0.0;
+    }
+    info[0] = n;
+    info[1] = s_h;
+    info[2] = s_h >= 0 ? counts[s_h] : 0;
+    info[3] = s_trials;
+  }
+}
+
+__global__ void pairs_to_points_kernel(const float* __restrict__ ka, const float* __restrict__ kb,
+                                       const int32_t* __restrict__ pairs, const int32_t* __restrict__ n_dev, int mx,
+                                       float* __restrict__ x, float* __restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = *n_dev;
+  if (i >= mx || i >= n) return;
+  int a = pairs[2 * i], b = pairs[2 * i + 1];
+  for (int q = 0; q < 3; ++q) {
+    x[3 * i + q] = ka[3 * a + q];
+    y[3 * i + q] = kb[3 * b + q];
+  }
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+}  // namespace tdm
+
+using namespace tdm;
+
+extern "C" size_t tdm_ransac_workspace_bytes(int32_t m_max, int32_t iterations) {
+  (void)m_max;
+  if (iterations < 0) return 0;
+  return align256(8) + align256((size_t)(iterations > 0 ? iterations : 1) * 4);
+}
+
+extern "C" tdm_status tdm_ransac(const float* x, const float* y, const int32_t* m_dev, int32_t m_max,
+                                 const tdm_ransac_params* prm, double* rt, int32_t* inliers, int32_t* info, void* ws,
+                                 size_t ws_bytes, tdm_stream s) {
+  TDM_REQUIRE(x && y && m_dev && prm && rt && inliers && info && ws, "tdm_ransac: null pointer");
+  TDM_REQUIRE(m_max >= 0 && prm->iterations >= 0 && prm->threshold > 0.0f, "tdm_ransac: bad parameters");
+  TDM_REQUIRE(ws_bytes >= tdm_ransac_workspace_bytes(m_max, prm->iterations), "tdm_ransac: workspace too small");
+  uint8_t* w = static_cast<uint8_t*>(ws);
+  unsigned long long* best = reinterpret_cast<unsigned long long*>(w);
+  int32_t* counts = reinterpret_cast<int32_t*>(w + align256(8));
+  TDM_CHECK_CUDA(cudaMemsetAsync(best, 0, 8, s));
+  const int iters = prm->iterations;
+  if (iters > 0) {
+    int smem_pts = m_max <= 4096 ? m_max : 0;  // 96 KB of correspondences at most
+    size_t smem = (size_t)6 * smem_pts * sizeof(float);
+    if (smem > 48 * 1024) {
+      TDM_CHECK_CUDA(cudaFuncSetAttribute(trials_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    trials_kernel<<<(iters + 255) / 256, 256, smem, s>>>(x, y, m_dev, m_max, smem_pts, prm->seed, iters,
+                                                          prm->threshold, counts, best);
+    TDM_CHECK_LAUNCH("trials_kernel");
+  }
+  finalize_kernel<<<1, 1024, 0, s>>>(x, y, m_dev, m_max, prm->seed, iters, prm->threshold, prm->adaptive ? 1 : 0,
+                                     prm->max_trials, counts, best, rt, inliers, info);
+  TDM_CHECK_LAUNCH("finalize_kernel");
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_pairs_to_points(const float* ka, const float* kb, const int32_t* pairs,
+                                          const int32_t* n_pairs, int32_t max_pairs, float* x, float* y,
+                                          tdm_stream s) {
+  TDM_REQUIRE(ka && kb && pairs && n_pairs && x && y && max_pairs >= 0, "tdm_pairs_to_points: bad arguments");
+  if (max_pairs == 0) return TDM_OK;
+  pairs_to_points_kernel<<<(max_pairs + 255) / 256, 256, 0, s>>>(ka, kb, pairs, n_pairs, max_pairs, x, y);
+  TDM_CHECK_LAUNCH("pairs_to_points_kernel");
+  return TDM_OK;
+}

@@ -1,0 +1,338 @@
+// TDF voxelisation, keypoint selection and 30^3 patch gather.
+//
+// Replaces core/demo.cu:97-218.  The reference's ComputeTDF (core/demo.cu:22-57)
+// scans an 11^3 cube per empty voxel (1,331 occupancy reads).  Here the same
+// value comes from an exact separable windowed squared distance computed in
+// shared-memory tiles:
+//   g1 = min_{|dx|<=r, occ} dx^2,  g2 = min_{|dy|<=r} dy^2 + g1,  g3 = min_{|dz|<=r} dz^2 + g2
+// which is the minimum of dx^2+dy^2+dz^2 over the occupied voxels of the cube.
+// Because sqrtf, /r and 1-x are monotone, 1 - sqrtf(g3)/r equals the
+// reference's running max of 1 - sqrtf(d^2)/r bit for bit (integer d^2 is
+// exact in float; sqrtf and the division are IEEE round-to-nearest).
+#include <climits>
+
+#include "common.cuh"
+
+namespace tdm {
+tdm_status grid_from_minmax(const float mn[3], const float mx[3], float vs, float trunc, int32_t pad, tdm_grid* g);
+}
+using namespace tdm;
+
+namespace {
+
+constexpr uint16_t kNone = 0xFFFF;
+
+__device__ __forceinline__ int float_to_ordered(float f) {
+  int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__host__ __device__ __forceinline__ float ordered_to_float(int i) {
+  int b = i >= 0 ? i : i ^ 0x7FFFFFFF;
+  float f;
+  memcpy(&f, &b, sizeof(f));
+  return f;
+}
+
+__global__ void minmax_init_kernel(int* ws) {
+  if (threadIdx.x < 3) ws[threadIdx.x] = INT_MAX;
+  else if (threadIdx.x < 6) ws[threadIdx.x] = INT_MIN;
+}
+
+__global__ __launch_bounds__(256) void minmax_kernel(const float* __restrict__ pts, int n, int* ws) {
+  float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      float v = pts[3 * (int64_t)i + a];
+      mn[a] = fminf(mn[a], v);
+      mx[a] = fmaxf(mx[a], v);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+      mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(ws + a, float_to_ordered(mn[a]));
+      atomicMax(ws + 3 + a, float_to_ordered(mx[a]));
+    }
+  }
+}
+
+// occ[z*dy*dx + y*dx + x] = 1, x = round((p - o)/vs)   (core/demo.cu:127-135)
+__global__ __launch_bounds__(256) void occupancy_kernel(const float* __restrict__ pts, int n, int dx, int dy, int dz,
+                                                        float ox, float oy, float oz, float vs,
+                                                        uint8_t* __restrict__ occ) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float px = pts[3 * (int64_t)i], py = pts[3 * (int64_t)i + 1], pz = pts[3 * (int64_t)i + 2];
+  int gx = (int)roundf(__fdiv_rn(__fsub_rn(px, ox), vs));
+  int gy = (int)roundf(__fdiv_rn(__fsub_rn(py, oy), vs));
+  int gz = (int)roundf(__fdiv_rn(__fsub_rn(pz, oz), vs));
+  if (gx < 0 || gy < 0 || gz < 0 || gx >= dx || gy >= dy || gz >= dz) return;
+  occ[((int64_t)gz * dy + gy) * dx + gx] = 1;
+}
+
+constexpr int TX = 32, TY = 8, TZ = 8;
+
+template <int R>
+__global__ __launch_bounds__(256) void tdf_tile_kernel(const uint8_t* __restrict__ occ, int dx, int dy, int dz,
+                                                       float* __restrict__ tdf) {
+  constexpr int IX = TX + 2 * R, IY = TY + 2 * R, IZ = TZ + 2 * R;
+  __shared__ uint8_t s_occ[IZ][IY][IX];
+  __shared__ uint16_t s_g1[IZ][IY][TX];
+  __shared__ uint16_t s_g2[IZ][TY][TX];
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  const int tid = threadIdx.x;
+
+  for (int i = tid; i < IX * IY * IZ; i += 256) {
+    int lx = i % IX, ly = (i / IX) % IY, lz = i / (IX * IY);
+    int gx = x0 - R + lx, gy = y0 - R + ly, gz = z0 - R + lz;
+    uint8_t v = 0;
+    if (gx >= 0 && gy >= 0 && gz >= 0 && gx < dx && gy < dy && gz < dz) v = occ[((int64_t)gz * dy + gy) * dx + gx];
+    s_occ[lz][ly][lx] = v;
+  }
+  __syncthreads();
+  for (int i = tid; i < TX * IY * IZ; i += 256) {  // along x
+    int lx = i % TX, ly = (i / TX) % IY, lz = i / (TX * IY);
+    int best = kNone;
+#pragma unroll
+    for (int d = -R; d <= R; ++d)
+      if (s_occ[lz][ly][lx + R + d]) best = min(best, d * d);
+    s_g1[lz][ly][lx] = (uint16_t)best;
+  }
+  __syncthreads();
+  for (int i = tid; i < TX * TY * IZ; i += 256) {  // along y
+    int lx = i % TX, ly = (i / TX) % TY, lz = i / (TX * TY);
+    int best = kNone;
+#pragma unroll
+    for (int d = -R; d <= R; ++d) {
+      int v = s_g1[lz][ly + R + d][lx];
+      if (v != kNone) best = min(best, v + d * d);
+    }
+    s_g2[lz][ly][lx] = (uint16_t)best;
+  }
+  __syncthreads();
+  for (int i = tid; i < TX * TY * TZ; i += 256) {  // along z, then the TDF value
+    int lx = i % TX, ly = (i / TX) % TY, lz = i / (TX * TY);
+    int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
+    if (gx >= dx || gy >= dy || gz >= dz) continue;
+    float out;
+    if (s_occ[lz + R][ly + R][lx + R]) {
+      out = 1.0f;
+    } else {
+      int best = kNone;
+#pragma unroll
+      for (int d = -R; d <= R; ++d) {
+        int v = s_g2[lz + R + d][ly][lx];
+        if (v != kNone) best = min(best, v + d * d);
+      }
+      out = 0.0f;
+      if (best != kNone) {
+        float v = __fsub_rn(1.0f, __fdiv_rn(__fsqrt_rn((float)best), (float)R));
+        out = v > 0.0f ? v : 0.0f;
+      }
+    }
+    tdf[((int64_t)gz * dy + gy) * dx + gx] = out;
+  }
+}
+
+// The reference decodes voxel_idx through float32 (core/demo.cu:32-34); above
+// 2^24 that lands on a different (x,y,z).  mode 1 evaluates its expressions
+// without contraction, mode 2 with nvcc's default a - b*c -> fma(-b, c, a).
+__device__ __forceinline__ void refcompat_decode(int64_t idx, int dx, int dy, int mode, int& x, int& y, int& z) {
+  float fi = (float)idx, fx = (float)dx, fy = (float)dy;
+  z = (int)floorf(__fdiv_rn(fi, __fmul_rn(fx, fy)));
+  float zp = __fmul_rn((float)z, fx);
+  float u = mode == 1 ? __fsub_rn(fi, __fmul_rn(zp, fy)) : __fmaf_rn(-zp, fy, fi);
+  y = (int)floorf(__fdiv_rn(u, fx));
+  float xr = mode == 1 ? __fsub_rn(u, __fmul_rn((float)y, fx)) : __fmaf_rn(-(float)y, fx, u);
+  x = (int)xr;
+}
+
+// Re-evaluates, for voxels >= 2^24 whose float decode differs from the exact
+// one, the reference loop around the mis-decoded centre (clipped window, max of
+// 1 - sqrtf(d^2)/r over occupied voxels, initial 0).
+__global__ __launch_bounds__(256) void tdf_refcompat_kernel(const uint8_t* __restrict__ occ, int dx, int dy, int dz,
+                                                            int r, int mode, int64_t v0, int64_t V,
+                                                            float* __restrict__ tdf) {
+  int64_t idx = v0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= V) return;
+  int64_t plane = (int64_t)dx * dy;
+  int ez = (int)(idx / plane);
+  int ey = (int)((idx - (int64_t)ez * plane) / dx);
+  int ex = (int)(idx - (int64_t)ez * plane - (int64_t)ey * dx);
+  int x, y, z;
+  refcompat_decode(idx, dx, dy, mode, x, y, z);
+  if ((x == ex && y == ey && z == ez) || occ[idx]) return;
+  float best = 0.0f;
+  int xa = max(0, x - r), xb = min(dx, x + r + 1);
+  int ya = max(0, y - r), yb = min(dy, y + r + 1);
+  int za = max(0, z - r), zb = min(dz, z + r + 1);
+  for (int iz = za; iz < zb; ++iz)
+    for (int iy = ya; iy < yb; ++iy)
+      for (int ix = xa; ix < xb; ++ix)
+        if (occ[((int64_t)iz * dy + iy) * dx + ix]) {
+          int d2 = (x - ix) * (x - ix) + (y - iy) * (y - iy) + (z - iz) * (z - iz);
+          float v = __fsub_rn(1.0f, __fdiv_rn(__fsqrt_rn((float)d2), (float)r));
+          if (v > best) best = v;
+        }
+  tdf[idx] = best;
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+__global__ void keypoint_index_kernel(uint64_t seed, uint32_t n_pts, int k, int32_t* idx) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k) return;
+  uint64_t r = mix64(seed + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ULL);
+  idx[i] = (int32_t)__umul64hi(r, (uint64_t)n_pts);
+}
+
+// keypts = pts[idx]; grid = round((p - o)/vs)   (core/demo.cu:168-176)
+__global__ void keypoint_kernel(const float* __restrict__ pts, int n_pts, const int32_t* __restrict__ idx, int k,
+                                float ox, float oy, float oz, float vs, float* __restrict__ keypts,
+                                int32_t* __restrict__ kp_grid, int* err) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k) return;
+  int j = idx[i];
+  if (j < 0 || j >= n_pts) {
+    atomicExch(err, DEV_BAD_INDEX);
+    j = 0;
+  }
+  float o[3] = {ox, oy, oz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float p = pts[3 * (int64_t)j + a];
+    keypts[3 * i + a] = p;
+    kp_grid[3 * i + a] = (int32_t)roundf(__fdiv_rn(__fsub_rn(p, o[a]), vs));
+  }
+}
+
+// patches[k][z][y][x] = tdf[kz-15+z][ky-15+y][kx-15+x]   (core/demo.cu:206-217)
+__global__ __launch_bounds__(256) void gather_kernel(const float* __restrict__ tdf, int dx, int dy, int dz,
+                                                     const int32_t* __restrict__ kp_grid,
+                                                     float* __restrict__ patches) {
+  const int k = blockIdx.x;
+  const int bx = kp_grid[3 * k] - 15, by = kp_grid[3 * k + 1] - 15, bz = kp_grid[3 * k + 2] - 15;
+  float* out = patches + (int64_t)k * 27000;
+  for (int i = threadIdx.x; i < 27000; i += 256) {
+    int x = i % 30, y = (i / 30) % 30, z = i / 900;
+    int gx = bx + x, gy = by + y, gz = bz + z;
+    float v = 0.0f;
+    if (gx >= 0 && gy >= 0 && gz >= 0 && gx < dx && gy < dy && gz < dz) v = __ldg(tdf + ((int64_t)gz * dy + gy) * dx + gx);
+    out[i] = v;
+  }
+}
+
+template <int R>
+void launch_tdf_tile(const uint8_t* occ, const tdm_grid* g, float* tdf, cudaStream_t s) {
+  dim3 grid((g->dim[0] + TX - 1) / TX, (g->dim[1] + TY - 1) / TY, (g->dim[2] + TZ - 1) / TZ);
+  tdf_tile_kernel<R><<<grid, 256, 0, s>>>(occ, g->dim[0], g->dim[1], g->dim[2], tdf);
+}
+
+int search_radius(const tdm_grid* g) { return (int)roundf(g->trunc_margin / g->voxel_size); }
+
+}  // namespace
+
+extern "C" size_t tdm_grid_workspace_bytes(void) { return 64; }
+
+extern "C" tdm_status tdm_grid_from_points(const float* pts, int32_t n, float vs, float trunc, int32_t pad,
+                                           tdm_grid* g, void* ws, tdm_stream s) {
+  TDM_REQUIRE(pts && g && ws && n > 0, "tdm_grid_from_points: null pointer or n <= 0");
+  int* w = static_cast<int*>(ws);
+  minmax_init_kernel<<<1, 32, 0, s>>>(w);
+  int blocks = (n + 255) / 256;
+  blocks = blocks > 1216 ? 1216 : blocks;
+  minmax_kernel<<<blocks, 256, 0, s>>>(pts, n, w);
+  TDM_CHECK_LAUNCH("minmax_kernel");
+  int h[6];
+  TDM_CHECK_CUDA(cudaMemcpyAsync(h, w, sizeof(h), cudaMemcpyDeviceToHost, s));
+  TDM_CHECK_CUDA(cudaStreamSynchronize(s));
+  float mn[3], mx[3];
+  for (int a = 0; a < 3; ++a) {
+    mn[a] = ordered_to_float(h[a]);
+    mx[a] = ordered_to_float(h[3 + a]);
+  }
+  return grid_from_minmax(mn, mx, vs, trunc, pad, g);
+}
+
+extern "C" size_t tdm_tdf_workspace_bytes(const tdm_grid* g) {
+  if (!g) return 0;
+  return (size_t)g->dim[0] * g->dim[1] * g->dim[2];
+}
+
+extern "C" tdm_status tdm_tdf(const float* pts, int32_t n, const tdm_grid* g, int32_t mode, float* tdf, void* ws,
+                              size_t ws_bytes, tdm_stream s) {
+  TDM_REQUIRE(pts && g && tdf && ws && n > 0, "tdm_tdf: null pointer or n <= 0");
+  TDM_REQUIRE(mode >= 0 && mode <= 2, "tdm_tdf: decode_mode must be 0, 1 or 2");
+  size_t V = tdm_tdf_workspace_bytes(g);
+  TDM_REQUIRE(V > 0 && ws_bytes >= V, "tdm_tdf: workspace too small");
+  int r = search_radius(g);
+  TDM_REQUIRE(r >= 1 && r <= 10, "tdm_tdf: trunc_margin/voxel_size must round to 1..10 voxels");
+  uint8_t* occ = static_cast<uint8_t*>(ws);
+  TDM_CHECK_CUDA(cudaMemsetAsync(occ, 0, V, s));
+  occupancy_kernel<<<(n + 255) / 256, 256, 0, s>>>(pts, n, g->dim[0], g->dim[1], g->dim[2], g->origin[0],
+                                                   g->origin[1], g->origin[2], g->voxel_size, occ);
+  TDM_CHECK_LAUNCH("occupancy_kernel");
+  switch (r) {
+    case 1: launch_tdf_tile<1>(occ, g, tdf, s); break;
+    case 2: launch_tdf_tile<2>(occ, g, tdf, s); break;
+    case 3: launch_tdf_tile<3>(occ, g, tdf, s); break;
+    case 4: launch_tdf_tile<4>(occ, g, tdf, s); break;
+    case 5: launch_tdf_tile<5>(occ, g, tdf, s); break;
+    case 6: launch_tdf_tile<6>(occ, g, tdf, s); break;
+    case 7: launch_tdf_tile<7>(occ, g, tdf, s); break;
+    case 8: launch_tdf_tile<8>(occ, g, tdf, s); break;
+    case 9: launch_tdf_tile<9>(occ, g, tdf, s); break;
+    default: launch_tdf_tile<10>(occ, g, tdf, s); break;
+  }
+  TDM_CHECK_LAUNCH("tdf_tile_kernel");
+  const int64_t first_bad = (int64_t)1 << 24;
+  if (mode != TDM_TDF_EXACT && (int64_t)V > first_bad) {
+    int64_t cnt = (int64_t)V - first_bad;
+    tdf_refcompat_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(occ, g->dim[0], g->dim[1], g->dim[2], r,
+                                                                        mode, first_bad, (int64_t)V, tdf);
+    TDM_CHECK_LAUNCH("tdf_refcompat_kernel");
+  }
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_keypoint_indices(uint64_t seed, int32_t n_pts, int32_t k, int32_t* idx, tdm_stream s) {
+  TDM_REQUIRE(idx && n_pts > 0 && k >= 0, "tdm_keypoint_indices: bad arguments");
+  if (k == 0) return TDM_OK;
+  keypoint_index_kernel<<<(k + 255) / 256, 256, 0, s>>>(seed, (uint32_t)n_pts, k, idx);
+  TDM_CHECK_LAUNCH("keypoint_index_kernel");
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_keypoints(const float* pts, int32_t n_pts, const int32_t* idx, int32_t k, const tdm_grid* g,
+                                    float* keypts, int32_t* kp_grid, tdm_stream s) {
+  TDM_REQUIRE(pts && idx && g && keypts && kp_grid && n_pts > 0 && k >= 0, "tdm_keypoints: bad arguments");
+  if (k == 0) return TDM_OK;
+  int* err = device_error_word();
+  if (!err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
+  keypoint_kernel<<<(k + 127) / 128, 128, 0, s>>>(pts, n_pts, idx, k, g->origin[0], g->origin[1], g->origin[2],
+                                                  g->voxel_size, keypts, kp_grid, err);
+  TDM_CHECK_LAUNCH("keypoint_kernel");
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_gather(const float* tdf, const tdm_grid* g, const int32_t* kp_grid, int32_t k, float* patches,
+                                 tdm_stream s) {
+  TDM_REQUIRE(tdf && g && kp_grid && patches && k >= 0, "tdm_gather: bad arguments");
+  if (k == 0) return TDM_OK;
+  gather_kernel<<<k, 256, 0, s>>>(tdf, g->dim[0], g->dim[1], g->dim[2], kp_grid, patches);
+  TDM_CHECK_LAUNCH("gather_kernel");
+  return TDM_OK;
+}

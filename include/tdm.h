@@ -1,0 +1,208 @@
+/*
+ * tdm.h -- C ABI of the GB300-native 3DMatch registration hot path.
+ *
+ * Every entry point returns a tdm_status, never exits and never traps.  Device
+ * pointers are caller-owned unless a handle says otherwise; every call is
+ * stream-ordered on the tdm_stream it is given (a cudaStream_t; NULL is the
+ * legacy default stream).  Calls that must return host-visible sizes say so.
+ *
+ * Each group cites the reference interface it replaces (andyzeng/3dmatch-toolbox
+ * paths).
+ */
+#ifndef TDM_H
+#define TDM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* tdm_stream; /* == cudaStream_t */
+
+typedef enum tdm_status {
+  TDM_OK = 0,
+  TDM_ERR_INVALID_ARG = 1,
+  TDM_ERR_IO = 2,
+  TDM_ERR_FORMAT = 3,
+  TDM_ERR_OOM = 4,
+  TDM_ERR_DEVICE = 5,
+  TDM_ERR_TIMEOUT = 6,
+  TDM_ERR_CANCELLED = 7,
+  TDM_ERR_UNSUPPORTED = 8
+} tdm_status;
+
+typedef enum tdm_precision {
+  TDM_FP32 = 0, /* CUDA-core FP32: the drop-in form */
+  TDM_BF16 = 1, /* tcgen05 BF16 operands, FP32 accumulation */
+  TDM_FP8 = 2   /* conv3..conv8 in FP8 E4M3 with per-channel weight scales; conv1/2 + feat BF16 */
+} tdm_precision;
+
+/* Voxel grid geometry of core/demo.cu:97-124: dims (x,y,z), origin of voxel
+ * (0,0,0), voxel size and truncation margin.  Voxel (x,y,z) is stored at
+ * z*dim[1]*dim[0] + y*dim[0] + x. */
+typedef struct tdm_grid {
+  int32_t dim[3];
+  float origin[3];
+  float voxel_size;
+  float trunc_margin;
+} tdm_grid;
+
+/* TDF index-decode modes (core/demo.cu:32-34 decodes the linear voxel index
+ * in float32, which is wrong above 2^24 voxels). */
+#define TDM_TDF_EXACT 0          /* exact integer decode (default) */
+#define TDM_TDF_REFCOMPAT_FLOAT 1 /* reference float32 decode, no contraction */
+#define TDM_TDF_REFCOMPAT_FMA 2  /* reference float32 decode with nvcc fmad contraction */
+
+/* ---- library ------------------------------------------------------------ */
+const char* tdm_version(void);
+/* Message of the last failing call on this host thread. */
+const char* tdm_last_error(void);
+/* Reads and clears the device-side error word (a bounded wait that ran out,
+ * an index that failed a check).  TDM_OK when clean; synchronizes `s`. */
+tdm_status tdm_device_status(tdm_stream s);
+
+/* ---- grid + TDF: replaces core/demo.cu:97-158 (ComputeTDF) ---------------- */
+/* Grid of core/demo.cu:97-124 from host points (float ops as the reference). */
+tdm_status tdm_grid_from_points_host(const float* pts_host, int32_t n, float voxel_size, float trunc_margin,
+                                     int32_t pad, tdm_grid* grid_out);
+/* Same from device points: min/max reduced on the device, then read back
+ * (synchronizes `s`).  ws_dev: tdm_grid_workspace_bytes() bytes. */
+size_t tdm_grid_workspace_bytes(void);
+tdm_status tdm_grid_from_points(const float* pts_dev, int32_t n, float voxel_size, float trunc_margin, int32_t pad,
+                                tdm_grid* grid_out, void* ws_dev, tdm_stream s);
+/* TDF of core/demo.cu:22-57 over the whole grid: occupancy scatter of the
+ * points, exact windowed squared distance, 1 - d/trunc.  tdf_dev: V floats.
+ * ws_dev: tdm_tdf_workspace_bytes(grid) bytes (occupancy). */
+size_t tdm_tdf_workspace_bytes(const tdm_grid* grid);
+tdm_status tdm_tdf(const float* pts_dev, int32_t n, const tdm_grid* grid, int32_t decode_mode, float* tdf_dev,
+                   void* ws_dev, size_t ws_bytes, tdm_stream s);
+
+/* ---- keypoints: replaces core/demo.cu:164-177 ----------------------------- */
+/* idx_i = floor(u_i * n_pts), u_i from splitmix64(seed, i) (the reference's
+ * random_device stream cannot be replayed, core/utils.hpp:15-20). */
+tdm_status tdm_keypoint_indices(uint64_t seed, int32_t n_pts, int32_t k, int32_t* idx_dev, tdm_stream s);
+/* keypts = pts[idx]; kp_grid = round((p - origin)/voxel_size) (int32 x,y,z). */
+tdm_status tdm_keypoints(const float* pts_dev, int32_t n_pts, const int32_t* idx_dev, int32_t k,
+                         const tdm_grid* grid, float* keypts_dev, int32_t* kp_grid_dev, tdm_stream s);
+
+/* ---- patch gather: replaces core/demo.cu:195-218 -------------------------- */
+/* patches[k][z][y][x] (30^3, x fastest) = tdf at kp_grid + (x,y,z) - 15; voxels
+ * outside the grid read 0. */
+tdm_status tdm_gather(const float* tdf_dev, const tdm_grid* grid, const int32_t* kp_grid_dev, int32_t k,
+                      float* patches_dev, tdm_stream s);
+
+/* ---- 3D ConvNet: replaces marvin::Net (core/demo.cu:179-231, core/marvin.hpp:
+ * 7434 init, 7596-7615 loadWeights, 7632 Malloc, 7653 forward) -------------- */
+typedef struct tdm_net tdm_net;
+/* Weights by Marvin name ("conv1.weight" [64,1,3,3,3] ... "feat.bias") from a
+ * .marvin file (core/marvin.hpp:2581-2612; half/float/double records).
+ * use_feat = 0 drops the final 1x1x1 `feat` layer (8-layer form). */
+tdm_status tdm_net_create(const char* marvin_path, tdm_precision precision, int32_t use_feat, tdm_net** out);
+/* Same from host arrays: weights[l] is [K][C][ks^3] float, biases[l] is [K]. */
+tdm_status tdm_net_create_from_host(const float* const* weights, const float* const* biases, tdm_precision precision,
+                                    int32_t use_feat, tdm_net** out);
+/* patches_dev: b x 27000 float (z,y,x);  desc_dev: b x 512 float. */
+tdm_status tdm_net_forward(tdm_net* net, const float* patches_dev, int32_t b, float* desc_dev, tdm_stream s);
+/* Net::getResponse(name) (core/marvin.hpp, used at core/demo.cu:185-186): runs
+ * the forward up to the named response ("conv1".."conv8", "pool1", "feat") and
+ * writes it as float, channels-last [b][D][D][D][C] (Marvin keeps NCDHW). */
+tdm_status tdm_net_response(tdm_net* net, const char* name, const float* patches_dev, int32_t b, float* out_dev,
+                            tdm_stream s);
+/* Patches per internal chunk (bounds the activation workspace; default 2048). */
+tdm_status tdm_net_set_max_batch(tdm_net* net, int32_t max_batch);
+tdm_status tdm_net_destroy(tdm_net* net);
+/* Seeded He-normal weights (N(0, 2/fan_in)), uniform biases in [-0.05, 0.05],
+ * written as float32 .marvin records. */
+tdm_status tdm_write_seeded_weights(const char* marvin_path, uint64_t seed);
+
+/* ---- mutual nearest neighbours: replaces core/demo.m:51-57 ---------------- */
+/* nn_ab[i] = argmin_j |a_i - b_j|, nn_ba likewise; pairs (nn_ba[j], j) for every
+ * j with nn_ab[nn_ba[j]] == j, in increasing j.  FP32: exact FP64 refinement of
+ * the FP32 candidates (indices equal the exact double-precision NN); BF16:
+ * tcgen05 distance GEMM.  pairs_dev: 2*min(na,nb) int32; n_pairs_dev: 1 int32. */
+size_t tdm_mnn_workspace_bytes(int32_t na, int32_t nb, int32_t dim);
+tdm_status tdm_match_mnn(const float* da_dev, int32_t na, const float* db_dev, int32_t nb, int32_t dim,
+                         tdm_precision precision, int32_t* nn_ab_dev, int32_t* nn_ba_dev, int32_t* pairs_dev,
+                         int32_t* n_pairs_dev, void* ws_dev, size_t ws_bytes, tdm_stream s);
+
+/* ---- RANSAC + rigid refit: replaces core/external/sfm/ransacfitRt.m:20-38,
+ * core/external/peter/ransac.m:113-232, estimateRt.m ------------------------ */
+typedef struct tdm_ransac_params {
+  uint64_t seed;      /* sample stream: splitmix64(seed, 3h+j) */
+  int32_t iterations; /* trials scored */
+  float threshold;    /* inlier if |x - (R y + t)| < threshold (strict) */
+  int32_t adaptive;   /* 1: replay ransac.m's adaptive stop (p=0.99) over the trials */
+  int32_t max_trials; /* adaptive cap (ransac.m default 50000) */
+} tdm_ransac_params;
+/* x = R y + t.  x_dev / y_dev: m_max x 3 float; the live count m is read from
+ * m_dev (device int32) so the call needs no host round trip.  rt_dev: 12
+ * doubles (3x4 row-major, FP64 Kabsch refit on the winner's inliers);
+ * inliers_dev: m_max int32; info_dev: 4 int32 = {n_inliers, best_trial,
+ * best_count, trials_run}. */
+size_t tdm_ransac_workspace_bytes(int32_t m_max, int32_t iterations);
+tdm_status tdm_ransac(const float* x_dev, const float* y_dev, const int32_t* m_dev, int32_t m_max,
+                      const tdm_ransac_params* params, double* rt_dev, int32_t* inliers_dev, int32_t* info_dev,
+                      void* ws_dev, size_t ws_bytes, tdm_stream s);
+/* x[i] = kp_a[pairs[2i]], y[i] = kp_b[pairs[2i+1]] for i < *n_pairs_dev. */
+tdm_status tdm_pairs_to_points(const float* kp_a_dev, const float* kp_b_dev, const int32_t* pairs_dev,
+                               const int32_t* n_pairs_dev, int32_t max_pairs, float* x_dev, float* y_dev,
+                               tdm_stream s);
+
+/* ---- TSDF fusion: replaces depth-fusion/demo.cu:18-68 (Integrate) and
+ * core/utils.hpp:23-65 (SaveVoxelGrid2SurfacePointCloud) -------------------- */
+/* tsdf = 1, weight = 0 (depth-fusion/demo.cu:131-135). */
+tdm_status tdm_tsdf_init(float* tsdf_dev, float* weight_dev, const int32_t dim[3], tdm_stream s);
+/* uint16 millimetres -> metres, > 6 m -> 0 (depth-fusion/utils.hpp ReadDepth). */
+tdm_status tdm_depth_from_mm(const uint16_t* mm_dev, int64_t n, float* depth_dev, tdm_stream s);
+/* Integrates n_frames depth maps (n_frames x height x width float metres) in
+ * order; cam2base_host: n_frames row-major 4x4 float; K: 3x3 row-major. */
+tdm_status tdm_tsdf_integrate(float* tsdf_dev, float* weight_dev, const int32_t dim[3], const float origin[3],
+                              float voxel_size, float trunc_margin, const float* depth_dev, int32_t n_frames,
+                              int32_t height, int32_t width, const float K[9], const float* cam2base_host,
+                              tdm_stream s);
+/* Voxel centres with |tsdf| < tsdf_thr and weight > w_thr, in linear index
+ * order; writes at most max_pts points, *n_pts_dev = total count. */
+size_t tdm_extract_workspace_bytes(const int32_t dim[3]);
+tdm_status tdm_tsdf_extract(const float* tsdf_dev, const float* weight_dev, const int32_t dim[3],
+                            const float origin[3], float voxel_size, float tsdf_thr, float w_thr, float* pts_dev,
+                            int64_t max_pts, int64_t* n_pts_dev, void* ws_dev, size_t ws_bytes, tdm_stream s);
+
+/* ---- whole path: core/demo.cu main + core/demo.m matching/registration ---- */
+typedef struct tdm_pipeline tdm_pipeline;
+typedef struct tdm_pipeline_config {
+  float voxel_size;      /* 0.01 */
+  float trunc_voxels;    /* 5 */
+  int32_t pad;           /* 15 */
+  int32_t max_points;    /* per fragment */
+  int32_t max_keypoints; /* per fragment */
+  int64_t max_voxels;    /* per fragment grid */
+  tdm_precision match_precision;
+  tdm_ransac_params ransac;
+} tdm_pipeline_config;
+typedef struct tdm_pair_result {
+  double rt[16];     /* 4x4, x_a = Rt * x_b */
+  int32_t n_matches; /* mutual-NN pairs */
+  int32_t n_inliers;
+  int32_t best_trial;
+  int32_t keypoints[2];
+  int32_t grid_dim[2][3];
+} tdm_pair_result;
+tdm_status tdm_pipeline_create(const tdm_pipeline_config* cfg, tdm_net* net, tdm_pipeline** out);
+tdm_status tdm_pipeline_destroy(tdm_pipeline* p);
+/* demo.cu for one fragment with device-resident points: grid, TDF, keypoints,
+ * gather, net.  keypts_dev: k x 3, desc_dev: k x 512 (caller-owned). */
+tdm_status tdm_describe_fragment(tdm_pipeline* p, const float* pts_dev, int32_t n, uint64_t kp_seed, int32_t k,
+                                 float* keypts_dev, float* desc_dev, tdm_grid* grid_out, tdm_stream s);
+/* Whole pair with device-resident points; result copied to host on return. */
+tdm_status tdm_register_pair(tdm_pipeline* p, const float* pts_a_dev, int32_t na, const float* pts_b_dev,
+                             int32_t nb, uint64_t seed, int32_t k, tdm_pair_result* result, tdm_stream s);
+/* Whole pair from host points (host->device copies inside the call). */
+tdm_status tdm_register_pair_host(tdm_pipeline* p, const float* pts_a_host, int32_t na, const float* pts_b_host,
+                                  int32_t nb, uint64_t seed, int32_t k, tdm_pair_result* result, tdm_stream s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TDM_H */

@@ -1,0 +1,122 @@
+"""GPU parity of the descriptor net against the oracle.
+
+Tolerances: FP32 form <= 1e-4 relative L2 against the FP32 oracle forward;
+BF16 tensor-core form <= 1e-2 relative L2 against the FP64 oracle forward.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RESPONSES = ["conv1", "conv2", "pool1", "conv3", "conv4", "conv5", "conv6", "conv7", "conv8", "feat"]
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.fixture(scope="module")
+def weights(oracle):
+    return oracle.he_normal_weights(20260001)
+
+
+@pytest.fixture(scope="module")
+def patches(tdm, oracle, scene, cuda):
+    """Real TDF patches of a synthetic fragment (the demo path)."""
+    import torch
+    pts = scene.fragment(20260002)
+    g = tdm.grid_from_points_host(pts)
+    pd = torch.from_numpy(pts).to(cuda)
+    tdf = tdm.tdf(pd, g)
+    idx = tdm.keypoint_indices(3, pts.shape[0], 12, device=cuda)
+    _, kg = tdm.keypoints(pd, idx, g)
+    return tdm.gather(tdf, g, kg)
+
+
+def _oracle_responses(oracle, p, w):
+    """Per-layer float64 responses, channels-last, via the oracle's conv loops."""
+    out = {}
+    x = p.reshape(-1, 30, 30, 30, 1).astype(np.float64)
+    B = x.shape[0]
+    D, C = 30, 1
+    for i, n in enumerate(oracle.NET_LAYERS):
+        K, ks = oracle.NET_COUT[i], oracle.NET_KS[i]
+        Do = D - ks + 1
+        y = np.zeros((B, Do, Do, Do, K))
+        lib = oracle.lib()
+        xin = np.ascontiguousarray(x)
+        wt = np.ascontiguousarray(w[n + ".weight"], np.float32)
+        bt = np.ascontiguousarray(w[n + ".bias"].reshape(-1), np.float32)
+        lib.orc_conv3d_f64(xin.ctypes.data, B, D, C, wt.ctypes.data, bt.ctypes.data, K, ks, 1 if i < 8 else 0,
+                           y.ctypes.data)
+        out[n] = y
+        x, D, C = y, Do, K
+        if i == 1:
+            Dp = D // 2
+            z = np.zeros((B, Dp, Dp, Dp, C))
+            lib.orc_pool_f64(np.ascontiguousarray(x).ctypes.data, B, D, C, z.ctypes.data)
+            out["pool1"] = z
+            x, D = z, Dp
+    return out
+
+
+@pytest.fixture(scope="module")
+def oracle_resp(oracle, patches, weights):
+    return _oracle_responses(oracle, patches.cpu().numpy()[:4], weights)
+
+
+def test_fp32_descriptors(tdm, oracle, weights, patches):
+    net = tdm.Net(weights, precision="fp32")
+    got = net.forward(patches).cpu().numpy()
+    want = oracle.net_forward(patches.cpu().numpy(), weights)
+    assert rel_l2(got, want) <= 1e-4
+    want64 = oracle.net_forward(patches.cpu().numpy(), weights, f64=True)
+    assert rel_l2(got, want64) <= 1e-4
+    tdm.device_status()
+
+
+@pytest.mark.parametrize("name", RESPONSES)
+def test_fp32_responses(tdm, weights, patches, oracle_resp, name):
+    net = tdm.Net(weights, precision="fp32")
+    got = net.response(name, patches[:4]).cpu().numpy()
+    assert rel_l2(got, oracle_resp[name]) <= 1e-5, name
+
+
+@pytest.mark.parametrize("name", RESPONSES)
+def test_bf16_responses(tdm, weights, patches, oracle_resp, name):
+    net = tdm.Net(weights, precision="bf16")
+    got = net.response(name, patches[:4]).cpu().numpy()
+    assert rel_l2(got, oracle_resp[name]) <= 1e-2, name
+    tdm.device_status()
+
+
+def test_bf16_descriptors(tdm, oracle, weights, patches):
+    net = tdm.Net(weights, precision="bf16")
+    got = net.forward(patches).cpu().numpy()
+    want64 = oracle.net_forward(patches.cpu().numpy(), weights, f64=True)
+    assert rel_l2(got, want64) <= 1e-2
+    tdm.device_status()
+
+
+def test_bf16_batch_independence(tdm, weights, patches):
+    """A patch's descriptor does not depend on its batch neighbours or chunking."""
+    import torch
+    net = tdm.Net(weights, precision="bf16")
+    full = net.forward(patches).cpu().numpy()
+    one = net.forward(patches[5:6].contiguous()).cpu().numpy()
+    assert np.array_equal(full[5:6], one)
+    net.set_max_batch(5)
+    chunked = net.forward(patches).cpu().numpy()
+    assert np.array_equal(full, chunked)
+
+
+def test_marvin_file_path(tdm, oracle, patches, tmp_path):
+    """Weights written by the library load by name like Marvin's loadWeights."""
+    p = str(tmp_path / "seeded.marvin")
+    tdm.write_seeded_weights(p, 99)
+    w = oracle.read_marvin(p)
+    assert w["conv1.weight"].shape == (64, 1, 3, 3, 3) and w["feat.bias"].shape == (1, 512, 1, 1, 1)
+    net = tdm.Net(marvin_path=p, precision="fp32")
+    got = net.forward(patches[:3]).cpu().numpy()
+    want = oracle.net_forward(patches[:3].cpu().numpy(), w)
+    assert rel_l2(got, want) <= 1e-4
