@@ -27,12 +27,12 @@ STATUS = {0: "OK", 1: "INVALID_ARG", 2: "IO", 3: "FORMAT", 4: "OOM", 5: "DEVICE"
 
 # Every symbol include/tdm.h declares (checked by the CPU tests).
 EXPORTS = [
-    "tdm_version", "tdm_last_error", "tdm_device_status",
+    "tdm_version", "tdm_last_error", "tdm_device_status", "tdm_launch_count",
     "tdm_grid_from_points_host", "tdm_grid_workspace_bytes", "tdm_grid_from_points",
     "tdm_tdf_workspace_bytes", "tdm_tdf",
     "tdm_keypoint_indices", "tdm_keypoints", "tdm_gather",
     "tdm_net_create", "tdm_net_create_from_host", "tdm_net_forward", "tdm_net_response", "tdm_net_set_max_batch",
-    "tdm_net_destroy", "tdm_write_seeded_weights",
+    "tdm_net_set_timing", "tdm_net_layer_times", "tdm_net_destroy", "tdm_write_seeded_weights",
     "tdm_mnn_workspace_bytes", "tdm_match_mnn",
     "tdm_ransac_workspace_bytes", "tdm_ransac", "tdm_pairs_to_points",
     "tdm_tsdf_init", "tdm_depth_from_mm", "tdm_tsdf_integrate", "tdm_extract_workspace_bytes", "tdm_tsdf_extract",
@@ -94,6 +94,7 @@ def lib():
         "tdm_version": (ctypes.c_char_p, []),
         "tdm_last_error": (ctypes.c_char_p, []),
         "tdm_device_status": (i32, [P]),
+        "tdm_launch_count": (i64, []),
         "tdm_grid_from_points_host": (i32, [P, i32, f32, f32, i32, G]),
         "tdm_grid_workspace_bytes": (sz, []),
         "tdm_grid_from_points": (i32, [P, i32, f32, f32, i32, G, P, P]),
@@ -107,6 +108,8 @@ def lib():
         "tdm_net_forward": (i32, [P, P, i32, P, P]),
         "tdm_net_response": (i32, [P, ctypes.c_char_p, P, i32, P, P]),
         "tdm_net_set_max_batch": (i32, [P, i32]),
+        "tdm_net_set_timing": (i32, [P, i32]),
+        "tdm_net_layer_times": (i32, [P, P, P, i32]),
         "tdm_net_destroy": (i32, [P]),
         "tdm_write_seeded_weights": (i32, [ctypes.c_char_p, u64]),
         "tdm_mnn_workspace_bytes": (sz, [i32, i32, i32]),
@@ -162,6 +165,11 @@ def _stream(stream) -> int:
 
 def device_status(stream=None) -> None:
     check(lib().tdm_device_status(_stream(stream)))
+
+
+def launch_count() -> int:
+    """Kernels launched by libtdm so far in this process."""
+    return int(lib().tdm_launch_count())
 
 
 # --------------------------------------------------------------------------
@@ -263,6 +271,18 @@ class Net:
 
     def set_max_batch(self, n: int) -> None:
         check(lib().tdm_net_set_max_batch(self.handle, n))
+
+    LAYER_SLOTS = ["conv1", "conv2", "conv3", "conv4", "conv5", "conv6", "conv7", "conv8", "feat", "pool1"]
+
+    def set_timing(self, enable: bool) -> None:
+        check(lib().tdm_net_set_timing(self.handle, 1 if enable else 0))
+
+    def layer_times(self, reset: bool = False) -> dict:
+        """{layer: (total ms, launches)} from the CUDA events of set_timing(True)."""
+        ms = np.zeros(10, np.float64)
+        n = np.zeros(10, np.int64)
+        check(lib().tdm_net_layer_times(self.handle, _ptr(ms), _ptr(n), 1 if reset else 0))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.LAYER_SLOTS)}
 
     def close(self):
         if self.handle:

@@ -1,5 +1,6 @@
 // Library-level entry points: version, error reporting, device error word,
 // and the voxel-grid geometry of core/demo.cu:97-124.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -11,8 +12,11 @@
 namespace tdm {
 
 static thread_local std::string g_last_error;
+static std::atomic<int64_t> g_launches{0};
 
 void set_error(const std::string& msg) { g_last_error = msg; }
+
+void note_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 tdm_status fail(tdm_status st, const std::string& msg) {
   set_error(msg);
@@ -47,6 +51,8 @@ using namespace tdm;
 extern "C" const char* tdm_version(void) { return "tdm-gb300 0.1 (sm_103a)"; }
 
 extern "C" const char* tdm_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int64_t tdm_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 extern "C" tdm_status tdm_device_status(tdm_stream s) {
   int* w = device_error_word();

@@ -36,8 +36,15 @@ enum DeviceError : int {
     if (_e != cudaSuccess) return ::tdm::cuda_status(_e, #expr);          \
   } while (0)
 
+namespace tdm {
+// Process-wide count of kernels this library has launched (tdm_launch_count).
+void note_launches(int n);
+}  // namespace tdm
+
+// Checks the launch that just happened and counts it.
 #define TDM_CHECK_LAUNCH(what)                                            \
   do {                                                                    \
+    ::tdm::note_launches(1);                                              \
     cudaError_t _e = cudaGetLastError();                                  \
     if (_e != cudaSuccess) return ::tdm::cuda_status(_e, what);           \
   } while (0)

@@ -10,56 +10,73 @@
 namespace tdm {
 namespace {
 
-// conv1: 1 -> 64 channels, 30^3 -> 28^3, bias + ReLU.  Thread = (output
-// position, group of 16 channels); weights [27][64] staged in shared memory.
+// conv1: 1 -> 64 channels, 30^3 -> 28^3, bias + ReLU.  Thread = (4
+// consecutive x positions, group of 16 channels): per tap, 16 weights read
+// from shared memory as float4 feed 64 FMAs.  Weights [27][64] in shared memory.
 template <bool BF16_OUT>
-__global__ __launch_bounds__(256) void conv1_kernel(const float* __restrict__ patches, int64_t n_pos,
+__global__ __launch_bounds__(256) void conv1_kernel(const float* __restrict__ patches, int64_t n_quads,
                                                     const float* __restrict__ w, const float* __restrict__ bias,
                                                     void* __restrict__ out, int64_t out_cs) {
-  __shared__ float sw[27 * 64];
+  __shared__ __align__(16) float sw[27 * 64];
   __shared__ float sb[64];
   for (int i = threadIdx.x; i < 27 * 64; i += 256) sw[i] = w[i];
   if (threadIdx.x < 64) sb[threadIdx.x] = bias[threadIdx.x];
   __syncthreads();
-  const int64_t pos = (int64_t)blockIdx.x * 64 + threadIdx.x / 4;
+  const int64_t q = (int64_t)blockIdx.x * 64 + threadIdx.x / 4;  // x-quad index
   const int g = threadIdx.x & 3;
-  if (pos >= n_pos) return;
-  const int64_t b = pos / 21952;
-  const int r = (int)(pos - b * 21952);
-  const int z = r / 784, y = (r / 28) % 28, x = r % 28;
-  const float* p = patches + b * 27000 + z * 900 + y * 30 + x;
-  float acc[16];
+  if (q >= n_quads) return;
+  const int64_t b = q / 5488;  // 28 * 28 * 7 quads per patch
+  const int r = (int)(q - b * 5488);
+  const int z = r / 196, y = (r / 7) % 28, x0 = (r % 7) * 4;
+  const float* p = patches + b * 27000 + z * 900 + y * 30 + x0;
+  float acc[4][16];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) acc[k] = sb[g * 16 + k];
+  for (int i = 0; i < 4; ++i)
 #pragma unroll
-  for (int t = 0; t < 27; ++t) {
-    const float v = __ldg(p + (t / 9) * 900 + ((t / 3) % 3) * 30 + (t % 3));
-    const float* wt = sw + t * 64 + g * 16;
+    for (int k = 0; k < 16; ++k) acc[i][k] = sb[g * 16 + k];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) acc[k] = fmaf(v, wt[k], acc[k]);
-  }
+  for (int zy = 0; zy < 9; ++zy) {
+    const float* row = p + (zy / 3) * 900 + (zy % 3) * 30;
+    float v[6];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) acc[k] = fmaxf(acc[k], 0.0f);
-  if (BF16_OUT) {
-    // channels-in-chunks-of-8 planar layout: chunk j at out + j*out_cs, row pos at +pos*16
+    for (int j = 0; j < 6; ++j) v[j] = __ldg(row + j);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      uint4 q;
-      __nv_bfloat162 t0 = __floats2bfloat162_rn(acc[8 * h + 0], acc[8 * h + 1]);
-      __nv_bfloat162 t1 = __floats2bfloat162_rn(acc[8 * h + 2], acc[8 * h + 3]);
-      __nv_bfloat162 t2 = __floats2bfloat162_rn(acc[8 * h + 4], acc[8 * h + 5]);
-      __nv_bfloat162 t3 = __floats2bfloat162_rn(acc[8 * h + 6], acc[8 * h + 7]);
-      q.x = *reinterpret_cast<uint32_t*>(&t0);
-      q.y = *reinterpret_cast<uint32_t*>(&t1);
-      q.z = *reinterpret_cast<uint32_t*>(&t2);
-      q.w = *reinterpret_cast<uint32_t*>(&t3);
-      uint8_t* dst = static_cast<uint8_t*>(out) + (int64_t)(2 * g + h) * out_cs + pos * 16;
-      *reinterpret_cast<uint4*>(dst) = q;
+    for (int dx = 0; dx < 3; ++dx) {
+      const float4* wt = reinterpret_cast<const float4*>(sw + (zy * 3 + dx) * 64 + g * 16);
+      float wk[16];
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        float4 t = wt[h];
+        wk[4 * h] = t.x; wk[4 * h + 1] = t.y; wk[4 * h + 2] = t.z; wk[4 * h + 3] = t.w;
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 16; ++k) acc[i][k] = fmaf(v[i + dx], wk[k], acc[i][k]);
     }
-  } else {
-    float4* dst = reinterpret_cast<float4*>(static_cast<float*>(out) + pos * 64 + g * 16);
+  }
+  const int64_t pos0 = b * 21952 + (int64_t)(z * 28 + y) * 28 + x0;
 #pragma unroll
-    for (int h = 0; h < 4; ++h) dst[h] = make_float4(acc[4 * h], acc[4 * h + 1], acc[4 * h + 2], acc[4 * h + 3]);
+  for (int i = 0; i < 4; ++i) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[i][k] = fmaxf(acc[i][k], 0.0f);
+    const int64_t pos = pos0 + i;
+    if (BF16_OUT) {
+      // chunk-planar layout: chunk j at out + j*out_cs, row pos at +pos*16
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        __nv_bfloat162 t[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) t[e] = __floats2bfloat162_rn(acc[i][8 * h + 2 * e], acc[i][8 * h + 2 * e + 1]);
+        uint8_t* dst = static_cast<uint8_t*>(out) + (int64_t)(2 * g + h) * out_cs + pos * 16;
+        *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<uint4*>(t);
+      }
+    } else {
+      float4* dst = reinterpret_cast<float4*>(static_cast<float*>(out) + pos * 64 + g * 16);
+#pragma unroll
+      for (int h = 0; h < 4; ++h)
+        dst[h] = make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]);
+    }
   }
 }
 
@@ -227,10 +244,10 @@ __global__ __launch_bounds__(256) void pool_c8_kernel(const uint8_t* __restrict_
 
 tdm_status launch_conv1(const float* patches, int B, const float* w, const float* bias, bool bf16_out, void* out,
                         int64_t out_cs, cudaStream_t s) {
-  int64_t n_pos = (int64_t)B * 21952;
-  unsigned blocks = (unsigned)((n_pos + 63) / 64);
-  if (bf16_out) conv1_kernel<true><<<blocks, 256, 0, s>>>(patches, n_pos, w, bias, out, out_cs);
-  else conv1_kernel<false><<<blocks, 256, 0, s>>>(patches, n_pos, w, bias, out, out_cs);
+  int64_t n_quads = (int64_t)B * 5488;
+  unsigned blocks = (unsigned)((n_quads + 63) / 64);
+  if (bf16_out) conv1_kernel<true><<<blocks, 256, 0, s>>>(patches, n_quads, w, bias, out, out_cs);
+  else conv1_kernel<false><<<blocks, 256, 0, s>>>(patches, n_quads, w, bias, out, out_cs);
   TDM_CHECK_LAUNCH("conv1_kernel");
   return TDM_OK;
 }

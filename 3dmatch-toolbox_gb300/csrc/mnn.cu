@@ -268,6 +268,7 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
   sqnorm_kernel<<<(nb + 7) / 8, 256, 0, s>>>(db, nb, dim, bn);
   max_kernel<<<1, 1024, 0, s>>>(an, na, maxes);
   max_kernel<<<1, 1024, 0, s>>>(bn, nb, maxes + 1);
+  note_launches(3);
   TDM_CHECK_LAUNCH("mnn norms");
   float* zeros = reinterpret_cast<float*>(w + L.zeros);
   TDM_CHECK_CUDA(cudaMemsetAsync(zeros, 0, (size_t)L.nbp * 4, s));
@@ -286,6 +287,7 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
     to_c8_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(da, na, dim, a8, L.a8_cs);
     n = (int64_t)L.nbp * (dim / 8);
     pack_b_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(db, nb, L.nbp, dim, bpk);
+    note_launches(1);
     TDM_CHECK_LAUNCH("mnn bf16 packing");
     TcLayer T{};
     T.cin = dim;
@@ -312,6 +314,7 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
   // rows: a -> b ; columns: b -> a (dot read transposed)
   nn_rows_kernel<<<(na + 7) / 8, 256, 0, s>>>(dot, L.nbp, na, nb, an, bn, maxes + 1, da, db, dim, 0, exact, nn_ab);
   nn_rows_kernel<<<(nb + 7) / 8, 256, 0, s>>>(dot, L.nbp, nb, na, bn, an, maxes, db, da, dim, 1, exact, nn_ba);
+  note_launches(1);
   TDM_CHECK_LAUNCH("nn_rows_kernel");
   mutual_kernel<<<1, 992, 0, s>>>(nn_ab, nn_ba, na, nb, pairs, n_pairs);
   TDM_CHECK_LAUNCH("mutual_kernel");

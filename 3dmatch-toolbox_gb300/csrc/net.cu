@@ -31,6 +31,8 @@ constexpr int kDefaultMaxBatch = 2048;
 // Response ids: layer index 0..8 (conv1..conv8, feat) = that layer's output
 // (after its in-place ReLU); kPool = pool1.  -1 = the full forward.
 constexpr int kPool = 100;
+// timed layer ids: 0..8 = conv1..feat, 9 = pool1
+constexpr int kTimedLayers = 10;
 
 // Chunk-planar BF16 -> channels-last float (responses of the BF16 form).
 // taps_layout: rows are patches and chunk = tap*(C/8) + c/8 (conv7's output).
@@ -68,10 +70,53 @@ struct tdm_net {
   uint8_t* ws = nullptr;
   size_t ws_bytes = 0;
   int max_batch = kDefaultMaxBatch;
+  // optional per-layer timing: CUDA events recorded on the launching stream
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+  std::vector<std::pair<int, size_t>> ev_pending;  // (layer id, pool slot)
+  double layer_ms[kTimedLayers] = {};
+  int64_t layer_n[kTimedLayers] = {};
 
   ~tdm_net() {
     for (void* p : allocs) cudaFree(p);
     if (ws) cudaFree(ws);
+    for (auto& e : ev_pool) {
+      cudaEventDestroy(e.first);
+      cudaEventDestroy(e.second);
+    }
+  }
+  // Folds recorded event pairs into the per-layer totals (synchronizes).
+  cudaError_t drain() {
+    for (auto& pe : ev_pending) {
+      auto& e = ev_pool[pe.second];
+      cudaError_t r = cudaEventSynchronize(e.second);
+      if (r != cudaSuccess) return r;
+      float t = 0.0f;
+      r = cudaEventElapsedTime(&t, e.first, e.second);
+      if (r != cudaSuccess) return r;
+      layer_ms[pe.first] += t;
+      layer_n[pe.first] += 1;
+    }
+    ev_pending.clear();
+    return cudaSuccess;
+  }
+  // Brackets one layer launch with events when timing is on.
+  cudaEvent_t begin(int id, cudaStream_t s) {
+    if (!timing) return nullptr;
+    if (ev_pending.size() >= 1024 && drain() != cudaSuccess) return nullptr;
+    size_t slot = ev_pending.size();
+    if (slot >= ev_pool.size()) {
+      cudaEvent_t a, b;
+      if (cudaEventCreate(&a) != cudaSuccess) return nullptr;
+      if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return nullptr; }
+      ev_pool.emplace_back(a, b);
+    }
+    ev_pending.emplace_back(id, slot);
+    cudaEventRecord(ev_pool[slot].first, s);
+    return ev_pool[slot].second;
+  }
+  void end(cudaEvent_t e, cudaStream_t s) {
+    if (e) cudaEventRecord(e, s);
   }
   template <typename T>
   tdm_status upload(const T* h, size_t n, T** d) {
@@ -183,7 +228,9 @@ tdm_status copy_response_f32(const float* src, int B, int id, float* out, cudaSt
 tdm_status forward_f32(tdm_net* net, const float* patches, int B, float* desc, int stop, cudaStream_t s) {
   float* b0 = reinterpret_cast<float*>(net->ws);
   float* b1 = b0 + (size_t)B * 1404928;  // 28^3 * 64
+  cudaEvent_t ev = net->begin(0, s);
   tdm_status st = launch_conv1(patches, B, net->d_w1, net->d_b[0], false, b0, 0, s);
+  net->end(ev, s);
   if (st) return st;
   if (stop == 0) return copy_response_f32(b0, B, 0, desc, s);
   float* in = b0;
@@ -192,11 +239,15 @@ tdm_status forward_f32(tdm_net* net, const float* patches, int B, float* desc, i
     if (l == 8 && !net->use_feat) break;
     bool last = stop < 0 && ((l == 8) || (l == 7 && !net->use_feat));
     float* dst = last ? desc : out;
+    ev = net->begin(l, s);
     st = launch_conv_f32(in, B, kDin[l], kCin[l], kKs[l], net->d_w32[l], net->d_b[l], kCout[l], l < 8, dst, s);
+    net->end(ev, s);
     if (st) return st;
     if (stop == l) return copy_response_f32(dst, B, l, desc, s);
     if (l == 1) {  // 2^3 max-pool after conv2 (26^3 -> 13^3)
+      ev = net->begin(9, s);
       st = launch_pool_f32(dst, B, 26, 64, in, s);
+      net->end(ev, s);
       if (st) return st;
       if (stop == kPool) return copy_response_f32(in, B, kPool, desc, s);
       continue;  // pooled result is back in `in`
@@ -253,7 +304,9 @@ tdm_status forward_bf16(tdm_net* net, const float* patches, int B, float* desc, 
   uint8_t* b1 = net->ws + P.off1;
   // conv1 -> chunk-planar BF16 input of conv2
   int64_t cs = P.rows_alloc[1] * 16;
+  cudaEvent_t ev = net->begin(0, s);
   tdm_status st = launch_conv1(patches, B, net->d_w1, net->d_b[0], true, b0, cs, s);
+  net->end(ev, s);
   if (st) return st;
   if (stop == 0) return c8_response(b0, cs, B, 0, false, desc, s);
   uint8_t* cur = b0;
@@ -282,13 +335,17 @@ tdm_status forward_bf16(tdm_net* net, const float* patches, int B, float* desc, 
       a.out = dst;
       a.out_cs = out_cs;
     }
+    ev = net->begin(l, s);
     st = launch_tc_layer(L, a, s);
+    net->end(ev, s);
     if (st) return st;
     if (last) break;
     if (stop == l) return c8_response(dst, out_cs, B, l, L.out_mode == TC_OUT_C8_TAPS, desc, s);
     if (l == 1) {  // pool 26^3 -> 13^3 back into buffer 0 as conv3's input
       int64_t pcs = P.rows_alloc[2] * 16;
+      ev = net->begin(9, s);
       st = launch_pool_c8(dst, out_cs, B, 26, 8, cur, pcs, s);
+      net->end(ev, s);
       if (st) return st;
       if (stop == kPool) return c8_response(cur, pcs, B, kPool, false, desc, s);
       cur_cs = pcs;
@@ -409,6 +466,26 @@ extern "C" tdm_status tdm_net_response(tdm_net* net, const char* name, const flo
 extern "C" tdm_status tdm_net_set_max_batch(tdm_net* net, int32_t max_batch) {
   TDM_REQUIRE(net && max_batch > 0, "tdm_net_set_max_batch: bad arguments");
   net->max_batch = max_batch;
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_net_set_timing(tdm_net* net, int32_t enable) {
+  TDM_REQUIRE(net, "tdm_net_set_timing: null net");
+  net->timing = enable != 0;
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_net_layer_times(tdm_net* net, double* ms, int64_t* launches, int32_t reset) {
+  TDM_REQUIRE(net && ms && launches, "tdm_net_layer_times: null pointer");
+  TDM_CHECK_CUDA(net->drain());
+  for (int i = 0; i < kTimedLayers; ++i) {
+    ms[i] = net->layer_ms[i];
+    launches[i] = net->layer_n[i];
+    if (reset) {
+      net->layer_ms[i] = 0.0;
+      net->layer_n[i] = 0;
+    }
+  }
   return TDM_OK;
 }
 

@@ -206,7 +206,7 @@ __global__ __launch_bounds__(1024) void finalize_kernel(const float* __restrict_
   __shared__ int s_h, s_trials, s_ok;
   __shared__ float sR[9], st[3];
   __shared__ int s_warp[32];
-  __shared__ int s_base;
+  __shared__ int s_base, s_round;
   int m = *m_dev;
   m = m < m_max ? m : m_max;
   if (threadIdx.x == 0) {
@@ -263,12 +263,12 @@ __global__ __launch_bounds__(1024) void finalize_kernel(const float* __restrict_
       if (threadIdx.x == 0) {
         int acc = 0;
         for (int q = 0; q < nw; ++q) { int t = s_warp[q]; s_warp[q] = acc; acc += t; }
-        s_warp[31] = acc;
+        s_round = acc;  // all 32 warps hold data: the total needs its own slot
       }
       __syncthreads();
       if (f) inliers[s_base + s_warp[w] + pre] = i;
       __syncthreads();
-      if (threadIdx.x == 0) s_base += s_warp[31];
+      if (threadIdx.x == 0) s_base += s_round;
       __syncthreads();
     }
   }

@@ -255,6 +255,7 @@ extern "C" tdm_status tdm_grid_from_points(const float* pts, int32_t n, float vs
   int blocks = (n + 255) / 256;
   blocks = blocks > 1216 ? 1216 : blocks;
   minmax_kernel<<<blocks, 256, 0, s>>>(pts, n, w);
+  note_launches(1);  // minmax_init_kernel
   TDM_CHECK_LAUNCH("minmax_kernel");
   int h[6];
   TDM_CHECK_CUDA(cudaMemcpyAsync(h, w, sizeof(h), cudaMemcpyDeviceToHost, s));

@@ -239,6 +239,7 @@ extern "C" tdm_status tdm_tsdf_extract(const float* tsdf, const float* w, const 
   extract_scan_kernel<<<1, 1024, 0, s>>>(cnt, nblk, offs, n_pts);
   extract_write_kernel<<<nblk, 256, 0, s>>>(tsdf, w, dim[0], dim[1], V, origin[0], origin[1], origin[2], vs, thr,
                                             wthr, offs, max_pts, pts);
+  note_launches(2);
   TDM_CHECK_LAUNCH("tsdf extract");
   return TDM_OK;
 }

@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""Pair registrations per second of the GB300 3DMatch registration path.
+
+A step registers one fragment pair shaped like the demo pipeline (two ~150k
+point fragments of a seeded synthetic room, 1 cm TDF, 1000 keypoints each,
+30^3 patches through the 9-layer net, mutual-NN matching, RANSAC with 100k
+trials and Kabsch refit).  The headline form is BF16 (tcgen05) for the net and
+the descriptor-distance GEMM; the FP32 CUDA-core form is timed beside it on the
+same GPU.  `value` is device-resident throughput (points already in HBM);
+`e2e` goes through the host C ABI (tdm_register_pair_host) with the
+host->device copy of the points and the device->host copy of the result
+inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference's loops (the
+C/OpenMP oracle) on the host cores on a bounded sample of the same workload,
+extrapolated to one pair.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONV2_FLOP_PER_PATCH = 2.0 * 26 ** 3 * 64 * (27 * 64)  # useful FLOPs of conv2 (algorithmic)
+NET_FLOP_PER_PATCH = 6.452e9
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
+    ap.add_argument("--keypoints", type=int, default=1000)
+    ap.add_argument("--points", type=int, default=150_000)
+    ap.add_argument("--ransac-iters", type=int, default=100_000)
+    ap.add_argument("--pairs", type=int, default=4, help="distinct synthetic pairs cycled through")
+    ap.add_argument("--fp32-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic(name):
+    """dram bytes per launch recorded in profiles/<name>.md ('traffic_bytes_per_launch: N')."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[4:8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the oracle's restated reference loops on a bounded sample
+# --------------------------------------------------------------------------
+def cpu_sample(pair, k, ransac_iters, scale):
+    """Times one bounded sample of the pair workload on the host cores and
+    extrapolates to a whole pair.  scale 1.0 ~ 10-20 s of CPU work."""
+    from oracle import oracle as O
+    O.set_threads(os.cpu_count() or 1)
+    a, b, _ = pair
+    t_tdf = 0.0
+    for pts in (a, b):
+        dim, origin = O.grid_setup(pts)
+        occ = O.occupancy(pts, dim, origin, 0.01)
+        V = int(np.prod(dim.astype(np.int64)))
+        nv = int(2_000_000 * scale)
+        v0 = V // 3
+        t0 = time.perf_counter()
+        O.tdf(occ, dim, 0.01, np.float32(0.01) * np.float32(5), 0, v0, v0 + nv)
+        t_tdf += (time.perf_counter() - t0) * V / nv
+    w = O.he_normal_weights(1)
+    npatch = max(1, int(8 * scale))
+    rng = np.random.default_rng(0)
+    patches = (rng.random((npatch, 27000)) * (rng.random((npatch, 27000)) < 0.15)).astype(np.float32)
+    t0 = time.perf_counter()
+    O.net_forward(patches, w)
+    t_net = (time.perf_counter() - t0) * (2 * k) / npatch
+    da = rng.normal(size=(k, 512)).astype(np.float32)
+    db = rng.normal(size=(k, 512)).astype(np.float32)
+    t0 = time.perf_counter()
+    O.mutual_nn(da, db)
+    t_mnn = time.perf_counter() - t0
+    m = 300
+    x = rng.uniform(-1, 1, (m, 3)).astype(np.float32)
+    y = rng.uniform(-1, 1, (m, 3)).astype(np.float32)
+    it = max(1000, int(ransac_iters * 0.2 * scale))
+    t0 = time.perf_counter()
+    O.ransac(x, y, 1, it, 0.05)
+    t_ransac = (time.perf_counter() - t0) * ransac_iters / it
+    t_pair = t_tdf + t_net + t_mnn + t_ransac
+    sample = ("TDF %d voxels x2 fragments (scaled to full grids), net %d patches (scaled to %d), "
+              "MNN %dx%d, RANSAC %d trials (scaled to %d), m=%d" % (int(2_000_000 * scale), npatch, 2 * k, k, k,
+                                                                    it, ransac_iters, m))
+    parts = {"tdf_s": t_tdf, "net_s": t_net, "mnn_s": t_mnn, "ransac_s": t_ransac}
+    return 1.0 / t_pair, sample, parts
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    import __graft_entry__ as ge
+    ge.load()
+    from tdm_gb300 import synth
+    pair = synth.fragment_pair(20260000, n_points=args.points)
+    scale = 0.15
+    for _ in range(args.warmup):
+        cpu_sample(pair, args.keypoints, args.ransac_iters, scale)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, sample, parts = cpu_sample(pair, args.keypoints, args.ransac_iters, scale)
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = float(np.mean(vals))
+    cores = os.cpu_count() or 1
+    line = {
+        "impl": "reference", "metric": "pair registrations/s", "value": value, "unit": "pairs/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "demo pipeline pair: 2 x %d-point synthetic room fragments, 1 cm TDF, %d keypoints "
+                               "per fragment, 30^3 patches, 9-layer net, mutual NN, RANSAC %d trials"
+                               % (args.points, args.keypoints, args.ransac_iters)},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
+                         "sample": sample + "; wall %.1fs for %d steps" % (wall, args.steps)},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference loops (oracle/oracle.c, OpenMP); the reference's own "
+                "demo.cu needs OpenCV and cuDNN and MATLAB for matching, so it is not built here",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def run_ours(args, rank, world, local):
+    import torch
+    import __graft_entry__ as ge
+    tdm = ge.load()
+    try:
+        tdm.lib()
+    except ImportError:
+        ge.build()
+        tdm.lib()
+    from tdm_gb300 import synth
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    k = args.keypoints
+    pairs = [synth.fragment_pair(20260000 + 97 * rank + i, n_points=args.points) for i in range(args.pairs)]
+    dpairs = [(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)) for a, b, _ in pairs]
+    hpairs = [(torch.from_numpy(a).pin_memory().numpy(), torch.from_numpy(b).pin_memory().numpy())
+              for a, b, _ in pairs]
+    wfile = os.path.join(tempfile.gettempdir(), "tdm_bench_weights_%d.marvin" % os.getpid())
+    tdm.write_seeded_weights(wfile, 20260000)
+
+    def make(prec):
+        net = tdm.Net(marvin_path=wfile, precision=prec)
+        pipe = tdm.Pipeline(net, max_keypoints=k, max_points=max(p[0].shape[0] for p in pairs) + 16,
+                            max_voxels=80_000_000, match_precision=prec, ransac_seed=20260000,
+                            ransac_iters=args.ransac_iters)
+        return net, pipe
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(pipe, steps, host=False):
+        stream = torch.cuda.current_stream()
+        barrier()
+        t0 = time.perf_counter()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        res = None
+        for s in range(steps):
+            if host:
+                a, b = hpairs[s % len(hpairs)]
+            else:
+                a, b = dpairs[s % len(dpairs)]
+            res = pipe.register(a, b, seed=1000 + s, k=k)
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1)
+        wall = (time.perf_counter() - t0) * 1000.0
+        t = torch.tensor([ms, wall], dtype=torch.float64, device=dev)
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t[0]), float(t[1]), res
+
+    prec = args.precision
+    net, pipe = make(prec)
+    for s in range(args.warmup):
+        a, b = dpairs[s % len(dpairs)]
+        pipe.register(a, b, seed=1000 + s, k=k)
+    net.layer_times(reset=True)
+    net.set_timing(True)
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = tdm.launch_count()
+    ms, wall, res = timed(pipe, args.steps)
+    launches = tdm.launch_count() - l0
+    clk = clocks.stop()
+    net.set_timing(False)
+    lt = net.layer_times(reset=True)
+    ms_step = ms / args.steps
+    value = world * args.steps / (ms / 1000.0)
+    # e2e through the host C ABI
+    e2e_steps = max(3, args.steps // 2)
+    ms_e2e, _, _ = timed(pipe, e2e_steps, host=True)
+    e2e = world * e2e_steps / (ms_e2e / 1000.0)
+    h2d = int(np.mean([(a.shape[0] + b.shape[0]) * 12 for a, b in hpairs]))
+    d2h = 12 * 8 + 16 + 4
+    # FP32 drop-in form on the same GPU
+    fp32 = None
+    if prec != "fp32" and args.fp32_steps > 0:
+        net32, pipe32 = make("fp32")
+        pipe32.register(*dpairs[0], seed=1, k=k)
+        ms32, _, _ = timed(pipe32, args.fp32_steps)
+        fp32 = world * args.fp32_steps / (ms32 / 1000.0)
+        pipe32.close()
+        net32.close()
+    # roofline of the dominant kernel: conv2 on tcgen05 (useful FLOPs per launch / event time)
+    conv2_ms, conv2_n = lt["conv2"]
+    peaks, peak_kind = load_peaks()
+    roof = None
+    if conv2_n > 0:
+        flop = CONV2_FLOP_PER_PATCH * 2 * k
+        achieved = flop / (conv2_ms / conv2_n / 1000.0) / 1e12
+        peak = peaks["bf16_tflops_sustained"] if prec == "bf16" else None
+        roof = {"kernel": "tc_conv_kernel<64,4> (conv2, %d patches per launch)" % (2 * k),
+                "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if peak else None, "peak_source": peak_kind + " bf16 sustained",
+                "traffic": profile_traffic("conv2_tc_bf16"),
+                "ms_per_launch": conv2_ms / conv2_n, "share_of_step": (conv2_ms / args.steps) / ms_step}
+    layer_ms = {name: round(v[0] / max(1, v[1]), 4) for name, v in lt.items() if v[1]}
+    out = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            v, sample, parts = cpu_sample(pairs[0], k, args.ransac_iters, 4.0)
+            cpu = {"value": v, "unit": "pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
+                   "sample": sample, "parts_s_per_pair": {kk: round(vv, 3) for kk, vv in parts.items()}}
+        out = {
+            "metric": "pair registrations/s", "value": value, "unit": "pairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": prec, "data": "synthetic",
+            "config": {"workload": "demo pipeline pair: 2 x %d-point synthetic room fragments, 1 cm TDF, %d keypoints "
+                                   "per fragment, 30^3 patches, 9-layer net (%s), mutual NN (%s), RANSAC %d trials, "
+                                   "Kabsch refit" % (args.points, k, prec, prec, args.ransac_iters),
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "working set > L2 (net activations %.1f GB per step)" % (2 * k * 5.1e6 / 1e9),
+                       "fp32_pairs_per_s": fp32,
+                       "bf16_over_fp32": (value / fp32) if fp32 else None,
+                       "net_tflops_useful": 2 * k * NET_FLOP_PER_PATCH / (ms_step / 1000.0) / 1e12,
+                       "layer_ms_per_launch": layer_ms,
+                       "last_result": {"matches": res.n_matches, "inliers": res.n_inliers} if res else None},
+            "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(out))
+    pipe.close()
+    net.close()
+    try:
+        os.unlink(wfile)
+    except OSError:
+        pass
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

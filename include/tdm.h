@@ -62,6 +62,9 @@ const char* tdm_last_error(void);
 /* Reads and clears the device-side error word (a bounded wait that ran out,
  * an index that failed a check).  TDM_OK when clean; synchronizes `s`. */
 tdm_status tdm_device_status(tdm_stream s);
+/* Number of kernels this library has launched in this process (diagnostics;
+ * the reference has no counterpart). */
+int64_t tdm_launch_count(void);
 
 /* ---- grid + TDF: replaces core/demo.cu:97-158 (ComputeTDF) ---------------- */
 /* Grid of core/demo.cu:97-124 from host points (float ops as the reference). */
@@ -112,6 +115,13 @@ tdm_status tdm_net_response(tdm_net* net, const char* name, const float* patches
                             tdm_stream s);
 /* Patches per internal chunk (bounds the activation workspace; default 2048). */
 tdm_status tdm_net_set_max_batch(tdm_net* net, int32_t max_batch);
+/* Per-layer device time, the analogue of Marvin's debug_mode tic/toc
+ * (core/marvin.hpp:445-456, 7656-7681): when enabled, every layer launch is
+ * bracketed by CUDA events on its stream.  tdm_net_layer_times synchronizes and
+ * returns accumulated milliseconds and launch counts for 10 slots (0..8 =
+ * conv1..conv8, feat; 9 = pool1); reset != 0 clears the totals. */
+tdm_status tdm_net_set_timing(tdm_net* net, int32_t enable);
+tdm_status tdm_net_layer_times(tdm_net* net, double* ms, int64_t* launches, int32_t reset);
 tdm_status tdm_net_destroy(tdm_net* net);
 /* Seeded He-normal weights (N(0, 2/fan_in)), uniform biases in [-0.05, 0.05],
  * written as float32 .marvin records. */

@@ -335,13 +335,29 @@ static double sqdist_f64(const float* a, const float* b, int dim) {
   return s;
 }
 
+/* Eight reference rows at a time: independent accumulation chains, each one
+ * still summed in k order, so every distance equals sqdist_f64's. */
 void orc_nn(const float* q, int nq, const float* ref, int nr, int dim, int32_t* nn) {
 #pragma omp parallel for schedule(dynamic, 8)
   for (int i = 0; i < nq; ++i) {
+    const float* a = q + (int64_t)i * dim;
     double best = INFINITY;
     int bj = 0;
-    for (int j = 0; j < nr; ++j) {
-      double d = sqdist_f64(q + (int64_t)i * dim, ref + (int64_t)j * dim, dim);
+    int j = 0;
+    for (; j + 8 <= nr; j += 8) {
+      double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (int k = 0; k < dim; ++k) {
+        double ak = (double)a[k];
+        for (int u = 0; u < 8; ++u) {
+          double d = ak - (double)ref[(int64_t)(j + u) * dim + k];
+          s[u] = fma(d, d, s[u]);
+        }
+      }
+      for (int u = 0; u < 8; ++u)
+        if (s[u] < best) { best = s[u]; bj = j + u; }
+    }
+    for (; j < nr; ++j) {
+      double d = sqdist_f64(a, ref + (int64_t)j * dim, dim);
       if (d < best) { best = d; bj = j; }
     }
     nn[i] = bj;
@@ -573,11 +589,14 @@ int orc_ransac_adaptive_stop(const int32_t* counts, int n_trials, int m, int max
 /* ------------------------------------------------------------------------ */
 /* TSDF integration, depth-fusion/demo.cu:18-68, one frame.                   */
 /* ------------------------------------------------------------------------ */
-void orc_tsdf_integrate(const float K[9], const float c2b[16], const float* depth, int H, int W, const int dim[3],
-                        const float origin[3], float vs, float trunc, float* tsdf, float* weight) {
+/* Voxels with z in [z0, z1) only (z1 <= 0 means all); tsdf/weight are the
+ * full grid arrays. */
+void orc_tsdf_integrate_z(const float K[9], const float c2b[16], const float* depth, int H, int W, const int dim[3],
+                          const float origin[3], float vs, float trunc, int z0, int z1, float* tsdf, float* weight) {
   int dx = dim[0], dy = dim[1], dz = dim[2];
+  if (z1 <= 0 || z1 > dz) z1 = dz;
 #pragma omp parallel for schedule(static)
-  for (int z = 0; z < dz; ++z)
+  for (int z = z0; z < z1; ++z)
     for (int y = 0; y < dy; ++y)
       for (int x = 0; x < dx; ++x) {
         float bx = origin[0] + (float)x * vs, by = origin[1] + (float)y * vs, bz = origin[2] + (float)z * vs;
@@ -600,6 +619,11 @@ void orc_tsdf_integrate(const float K[9], const float c2b[16], const float* dept
         weight[v] = wn;
         tsdf[v] = (tsdf[v] * wo + dist) / wn;
       }
+}
+
+void orc_tsdf_integrate(const float K[9], const float c2b[16], const float* depth, int H, int W, const int dim[3],
+                        const float origin[3], float vs, float trunc, float* tsdf, float* weight) {
+  orc_tsdf_integrate_z(K, c2b, depth, H, W, dim, origin, vs, trunc, 0, 0, tsdf, weight);
 }
 
 /* Surface points (core/utils.hpp:23-65): voxel centres o + i*vs where

@@ -83,6 +83,7 @@ def lib():
             "orc_ransac": (i32, [P, P, i32, u64, i32, f32, P, P, P, P]),
             "orc_ransac_adaptive_stop": (i32, [P, i32, i32, i32, P]),
             "orc_tsdf_integrate": (None, [P, P, P, i32, i32, P, P, f32, f32, P, P]),
+            "orc_tsdf_integrate_z": (None, [P, P, P, i32, i32, P, P, f32, f32, i32, i32, P, P]),
             "orc_extract_surface": (i64, [P, P, P, P, f32, f32, f32, P]),
         }
         for name, (res, args) in sig.items():
@@ -379,13 +380,16 @@ def estimate_rigid_transform_fp(x: np.ndarray, y: np.ndarray) -> np.ndarray:
 # --------------------------------------------------------------------------
 # TSDF
 # --------------------------------------------------------------------------
-def tsdf_integrate(K, cam2base, depth, dim, origin, vs, trunc, tsdf_grid, weight):
+def tsdf_integrate(K, cam2base, depth, dim, origin, vs, trunc, tsdf_grid, weight, z0=0, z1=0):
+    """One frame of depth-fusion/demo.cu:18-68 into the full grids (voxel
+    slices z0 <= z < z1 only, when z1 > 0)."""
     K = np.ascontiguousarray(K, np.float32).reshape(9)
     c2b = np.ascontiguousarray(cam2base, np.float32).reshape(16)
     depth = np.ascontiguousarray(depth, np.float32)
     H, W = depth.shape
-    lib().orc_tsdf_integrate(_p(K), _p(c2b), _p(depth), H, W, _p(np.ascontiguousarray(dim, np.int32)),
-                             _p(np.ascontiguousarray(origin, np.float32)), vs, trunc, _p(tsdf_grid), _p(weight))
+    lib().orc_tsdf_integrate_z(_p(K), _p(c2b), _p(depth), H, W, _p(np.ascontiguousarray(dim, np.int32)),
+                               _p(np.ascontiguousarray(origin, np.float32)), vs, trunc, z0, z1, _p(tsdf_grid),
+                               _p(weight))
 
 
 def extract_surface(tsdf_grid, weight, dim, origin, vs, tsdf_thr=0.2, w_thr=1.0):
