@@ -34,7 +34,7 @@ EXPORTS = [
     "tdm_net_create", "tdm_net_create_from_host", "tdm_net_forward", "tdm_net_response", "tdm_net_set_max_batch",
     "tdm_net_set_timing", "tdm_net_layer_times", "tdm_net_destroy", "tdm_write_seeded_weights",
     "tdm_mnn_workspace_bytes", "tdm_match_mnn",
-    "tdm_ransac_workspace_bytes", "tdm_ransac", "tdm_pairs_to_points",
+    "tdm_ransac_workspace_bytes", "tdm_ransac", "tdm_ransac_noalloc", "tdm_pairs_to_points",
     "tdm_tsdf_init", "tdm_depth_from_mm", "tdm_tsdf_integrate", "tdm_extract_workspace_bytes", "tdm_tsdf_extract",
     "tdm_pipeline_create", "tdm_pipeline_destroy", "tdm_describe_fragment", "tdm_register_pair",
     "tdm_register_pair_host",
@@ -116,6 +116,7 @@ def lib():
         "tdm_match_mnn": (i32, [P, i32, P, i32, i32, i32, P, P, P, P, P, sz, P]),
         "tdm_ransac_workspace_bytes": (sz, [i32, i32]),
         "tdm_ransac": (i32, [P, P, P, i32, ctypes.POINTER(RansacParams), P, P, P, P, sz, P]),
+        "tdm_ransac_noalloc": (i32, [P, P, P, i32, ctypes.POINTER(RansacParams), P, P, P, P]),
         "tdm_pairs_to_points": (i32, [P, P, P, P, i32, P, P, P]),
         "tdm_tsdf_init": (i32, [P, P, P, P]),
         "tdm_depth_from_mm": (i32, [P, i64, P, P]),

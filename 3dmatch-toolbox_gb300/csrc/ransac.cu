@@ -14,6 +14,9 @@
 // the same operations in the same order, so trial counts and inlier sets are
 // identical on both.
 #include <cfloat>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "common.cuh"
 
@@ -347,5 +350,88 @@ extern "C" tdm_status tdm_pairs_to_points(const float* ka, const float* kb, cons
   if (max_pairs == 0) return TDM_OK;
   pairs_to_points_kernel<<<(max_pairs + 255) / 256, 256, 0, s>>>(ka, kb, pairs, n_pairs, max_pairs, x, y);
   TDM_CHECK_LAUNCH("pairs_to_points_kernel");
+  return TDM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free RANSAC.
+//
+// tdm_ransac needs a caller-provided device workspace (the best-trial word and
+// one inlier count per trial).  Some callers cannot provide one: bindings that
+// reach this library through a foreign-function layer holding no device
+// allocator (a MATLAB loadlibrary/calllib binding, a scripting FFI that passes
+// only pointers it was given), and serving loops that forbid cudaMalloc after
+// start-up because it synchronizes the device and can fail under a memory
+// budget.  For them this variant keeps its scratch in a fixed device array of
+// this file, sized for kNoAllocMaxTrials trials (about 512 KB, held by every
+// GPU that loads the library until the process exits).
+//
+// The array is shared by every call: the best-trial word is cleared at the
+// start of each call and every trial count is rewritten, so a call never sees
+// the previous call's results, but two calls whose work overlaps on the GPU
+// (different streams, or different host threads) race on it and must be
+// serialized by the caller.
+// ---------------------------------------------------------------------------
+namespace tdm {
+namespace {
+
+constexpr int kNoAllocMaxTrials = 131072;
+constexpr size_t kNoAllocCountsOffset = 256;  // best word, padded; then counts
+static __device__ __align__(256) unsigned char g_ransac_scratch[kNoAllocCountsOffset + 4 * (size_t)kNoAllocMaxTrials];
+
+// Device address of g_ransac_scratch, resolved once per device with that
+// device current (the host-side symbol is only a stand-in, never a device
+// address).
+tdm_status noalloc_scratch(void** out) {
+  static std::mutex mu;
+  static std::vector<void*> addr;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)addr.size() <= dev) addr.resize(dev + 1, nullptr);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_ransac_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_ransac_scratch)");
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return TDM_OK;
+}
+
+}  // namespace
+}  // namespace tdm
+
+extern "C" tdm_status tdm_ransac_noalloc(const float* x, const float* y, const int32_t* m_dev, int32_t m_max,
+                                         const tdm_ransac_params* prm, double* rt, int32_t* inliers,
+                                         int32_t* info, tdm_stream s) {
+  TDM_REQUIRE(x && y && m_dev && prm && rt && inliers && info, "tdm_ransac_noalloc: null pointer");
+  TDM_REQUIRE(m_max >= 0 && prm->iterations >= 0 && prm->threshold > 0.0f, "tdm_ransac_noalloc: bad parameters");
+  if (prm->iterations > kNoAllocMaxTrials)
+    return fail(TDM_ERR_INVALID_ARG, "tdm_ransac_noalloc: iterations " + std::to_string(prm->iterations) +
+                                         " exceed the fixed scratch of " + std::to_string(kNoAllocMaxTrials) +
+                                         " trials; use tdm_ransac with a workspace");
+  void* scratch = nullptr;
+  tdm_status st = noalloc_scratch(&scratch);
+  if (st) return st;
+  uint8_t* w = static_cast<uint8_t*>(scratch);
+  unsigned long long* best = reinterpret_cast<unsigned long long*>(w);
+  int32_t* counts = reinterpret_cast<int32_t*>(w + kNoAllocCountsOffset);
+  TDM_CHECK_CUDA(cudaMemsetAsync(best, 0, 8, s));  // the best word must start at zero
+  const int iters = prm->iterations;
+  if (iters > 0) {
+    int smem_pts = m_max <= 4096 ? m_max : 0;
+    size_t smem = (size_t)6 * smem_pts * sizeof(float);
+    if (smem > 48 * 1024) {
+      TDM_CHECK_CUDA(cudaFuncSetAttribute(trials_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    trials_kernel<<<(iters + 255) / 256, 256, smem, s>>>(x, y, m_dev, m_max, smem_pts, prm->seed, iters,
+                                                          prm->threshold, counts, best);
+    TDM_CHECK_LAUNCH("trials_kernel (noalloc)");
+  }
+  finalize_kernel<<<1, 1024, 0, s>>>(x, y, m_dev, m_max, prm->seed, iters, prm->threshold, prm->adaptive ? 1 : 0,
+                                     prm->max_trials, counts, best, rt, inliers, info);
+  TDM_CHECK_LAUNCH("finalize_kernel (noalloc)");
   return TDM_OK;
 }

@@ -155,6 +155,20 @@ size_t tdm_ransac_workspace_bytes(int32_t m_max, int32_t iterations);
 tdm_status tdm_ransac(const float* x_dev, const float* y_dev, const int32_t* m_dev, int32_t m_max,
                       const tdm_ransac_params* params, double* rt_dev, int32_t* inliers_dev, int32_t* info_dev,
                       void* ws_dev, size_t ws_bytes, tdm_stream s);
+/* tdm_ransac without a caller workspace: no counterpart in the reference (its
+ * RANSAC is MATLAB).  For callers that cannot allocate device memory -- a
+ * foreign-function binding holding no device allocator, or a serving loop that
+ * forbids cudaMalloc after start-up -- the per-trial scratch lives in a fixed
+ * device array inside the library (about 512 KB per GPU that loads it, kept
+ * until the process exits).  Limit: params->iterations <= 131072 trials;
+ * larger values return TDM_ERR_INVALID_ARG.  The call allocates nothing.  Its
+ * first call on a device looks up the array's device address, so make that
+ * first call before any stream capture.  Every call shares the array (each
+ * call clears what must start at zero), so calls whose work overlaps on the
+ * GPU race and must be serialized by the caller.  Outputs as tdm_ransac. */
+tdm_status tdm_ransac_noalloc(const float* x_dev, const float* y_dev, const int32_t* m_dev, int32_t m_max,
+                              const tdm_ransac_params* params, double* rt_dev, int32_t* inliers_dev,
+                              int32_t* info_dev, tdm_stream s);
 /* x[i] = kp_a[pairs[2i]], y[i] = kp_b[pairs[2i+1]] for i < *n_pairs_dev. */
 tdm_status tdm_pairs_to_points(const float* kp_a_dev, const float* kp_b_dev, const int32_t* pairs_dev,
                                const int32_t* n_pairs_dev, int32_t max_pairs, float* x_dev, float* y_dev,
