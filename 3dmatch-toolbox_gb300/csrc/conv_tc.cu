@@ -20,10 +20,13 @@
 // (LBO = slab rows * 16 between K core matrices, SBO = 128 between 8-row
 // groups).  So each slab feeds 9 taps without re-staging.
 //
-// Roles (128 threads, one CTA per SM):
-//   warp 0 lane 0: producer (cp.async.bulk + mbarrier expect_tx)
-//   warp 1 lane 0: MMA issuer (tcgen05.mma, accumulators in TMEM), TMEM owner
-//   warps 0-3    : epilogue (tcgen05.ld, bias, ReLU, convert, store)
+// Roles (192 threads, one persistent CTA per SM walking the tiles):
+//   warp 0 lane 0: producer (cp.async.bulk + mbarrier expect_tx), continuous
+//                  across tile boundaries
+//   warp 1 lane 0: MMA issuer (tcgen05.mma into one of two TMEM accumulator
+//                  buffers), TMEM owner
+//   warps 2-5    : epilogue (tcgen05.ld, bias, ReLU, convert, store) of the
+//                  other buffer while the next tile accumulates
 // Every wait is bounded; a wait that runs out raises the device error word and
 // the CTA drains its in-flight copies, frees TMEM and exits.
 #include <cuda_fp8.h>
@@ -39,8 +42,11 @@
 namespace tdm {
 namespace {
 
-constexpr int NSA = 2;  // A slab stages
-constexpr int NSB = 4;  // B (weight) stages
+constexpr int NSA = 2;      // A slab stages
+constexpr int MAX_NSB = 12;  // B (weight) stages, sized from the shared-memory budget
+constexpr int kThreads = 192;  // warp 0 producer, warp 1 MMA + TMEM owner, warps 2-5 epilogue
+constexpr size_t kSmemLimit = 227 * 1024;
+constexpr size_t kSmemReserve = 512;  // barriers + TMEM address
 constexpr uint64_t kWaitBudgetNs = 500ull * 1000ull * 1000ull;
 
 struct KParams {
@@ -54,7 +60,8 @@ struct KParams {
   float out_qinv;
   uint8_t* out;
   int64_t out_cs;
-  int D, Do, nz, nyx, kgroups, cpg, cout, out_mode, relu, R;
+  int D, Do, nz, nyx, kgroups, cpg, cout, out_mode, relu, R, nsb, ntiles;
+  int64_t total_tiles;
   int* err;
 };
 
@@ -80,13 +87,19 @@ __device__ __forceinline__ bool wait_or_flag(uint32_t bar, uint32_t parity, int*
   }
 }
 
-__device__ __forceinline__ bool row_valid(const KParams& p, int64_t row) {
-  if (row >= p.rows) return false;
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// An M tile has no valid output row when it lies past the last input row or
+// entirely in the z >= Do tail of one patch (those tiles are skipped by every
+// role alike).
+__device__ __forceinline__ bool tile_has_work(const KParams& p, int64_t m0, int mcta) {
+  if (m0 >= p.rows) return false;
   if (p.nyx == 1) return true;
-  const int64_t D3 = (int64_t)p.D * p.D * p.D;
-  int r = (int)(row % D3);
-  int z = r / (p.D * p.D), y = (r / p.D) % p.D, x = r % p.D;
-  return x < p.Do && y < p.Do && z < p.Do;
+  const int64_t D2 = (int64_t)p.D * p.D, D3 = D2 * p.D;
+  const int64_t r0 = m0 % D3;
+  return !(r0 >= (int64_t)p.Do * D2 && r0 + mcta <= D3);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
@@ -105,36 +118,36 @@ __device__ __forceinline__ uint32_t pack_e4m3x4(float a, float b, float c, float
   return lo;
 }
 
+// Persistent, warp-specialised implicit-GEMM convolution.  Each CTA walks the
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ...; the load pipeline runs across
+// tile boundaries and the TMEM accumulator is double-buffered, so the epilogue
+// of one tile overlaps the MMAs of the next.
 template <int NT, int MSUB, bool FP8_IN, bool FP8_OUT>
-__global__ void __launch_bounds__(128, 1) tc_conv_kernel(const KParams p) {
+__global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr int MCTA = MSUB * 128;
-  constexpr uint32_t TMEM_COLS = tmem_cols_for(MSUB * NT);
-  const int R = p.R;
+  constexpr uint32_t ACC_COLS = MSUB * NT;  // one accumulator buffer
+  constexpr uint32_t TMEM_COLS = tmem_cols_for(2 * ACC_COLS);
+  static_assert(2 * ACC_COLS <= 512, "two accumulator buffers must fit in TMEM");
+  const int R = p.R, nsb = p.nsb;
   const uint32_t a_stage = 16u * (uint32_t)p.cpg * (uint32_t)R;
   constexpr uint32_t b_stage = NT * 128u;
   uint8_t* sA = smem;
   uint8_t* sB = smem + NSA * a_stage;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + NSB * b_stage);
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * NSA + 2 * NSB + 1);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + (size_t)nsb * b_stage);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * NSA + 2 * MAX_NSB + 5);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t m0 = (int64_t)blockIdx.x * MCTA;
-  const int ntile = blockIdx.y;
-  const int n0 = ntile * NT;
-
-  // Tiles with no valid output row do no work (the z >= Do tail of a patch).
-  int any = 0;
-  for (int i = threadIdx.x; i < MCTA; i += 128) any |= row_valid(p, m0 + i) ? 1 : 0;
-  if (!__syncthreads_or(any)) return;
   if (!__syncthreads_and(aborted(p.err) ? 0 : 1)) return;  // another CTA already failed
 
   const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * NSA;
-  const uint32_t fullB = emptyA + 8 * NSA, emptyB = fullB + 8 * NSB, accum = emptyB + 8 * NSB;
+  const uint32_t fullB = emptyA + 8 * NSA, emptyB = fullB + 8 * MAX_NSB;
+  const uint32_t accFull = emptyB + 8 * MAX_NSB, accEmpty = accFull + 16, done = accEmpty + 16;
   if (threadIdx.x == 0) {
     for (int i = 0; i < NSA; ++i) { ptx::mbar_init(fullA + 8 * i, 1); ptx::mbar_init(emptyA + 8 * i, 1); }
-    for (int i = 0; i < NSB; ++i) { ptx::mbar_init(fullB + 8 * i, 1); ptx::mbar_init(emptyB + 8 * i, 1); }
-    ptx::mbar_init(accum, 1);
+    for (int i = 0; i < nsb; ++i) { ptx::mbar_init(fullB + 8 * i, 1); ptx::mbar_init(emptyB + 8 * i, 1); }
+    for (int i = 0; i < 2; ++i) { ptx::mbar_init(accFull + 8 * i, 1); ptx::mbar_init(accEmpty + 8 * i, 4); }
+    ptx::mbar_init(done, 1);
     ptx::fence_barrier_init();
     ptx::fence_proxy_async_smem();
   }
@@ -149,152 +162,185 @@ __global__ void __launch_bounds__(128, 1) tc_conv_kernel(const KParams p) {
   const uint32_t sA_u = ptx::smem_u32(sA), sB_u = ptx::smem_u32(sB);
   const int64_t plane = (int64_t)p.D * p.D;
 
-  if (warp == 0 && lane == 0) {
-    // ---------------- producer ----------------
-    int sa = 0, sb = 0;
-    uint32_t pha = 0, phb = 0;
-    int armedA[NSA], armedB[NSB];  // parity of each stage's last arming, -1 = never
-    for (int i = 0; i < NSA; ++i) armedA[i] = -1;
-    for (int i = 0; i < NSB; ++i) armedB[i] = -1;
-    bool ok = true;
-    for (int zt = 0; zt < p.nz && ok; ++zt) {
-      for (int cg = 0; cg < p.kgroups && ok; ++cg) {
-        if (!wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
-        ptx::mbar_arrive_expect_tx(fullA + 8 * sa, a_stage);
-        armedA[sa] = (int)pha;
-        const uint8_t* src = p.act + (int64_t)cg * p.cpg * p.act_cs + (m0 + zt * plane) * 16;
-        for (int j = 0; j < p.cpg; ++j)
-          ptx::bulk_g2s(sA_u + sa * a_stage + j * R * 16, src + j * p.act_cs, R * 16, fullA + 8 * sa);
-        if (++sa == NSA) { sa = 0; pha ^= 1; }
-        for (int yx = 0; yx < p.nyx; ++yx) {
-          if (!wait_or_flag(emptyB + 8 * sb, phb ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
-          ptx::mbar_arrive_expect_tx(fullB + 8 * sb, b_stage);
-          armedB[sb] = (int)phb;
-          const int64_t blk = (((int64_t)ntile * p.nz + zt) * p.kgroups + cg) * p.nyx + yx;
-          ptx::bulk_g2s(sB_u + sb * b_stage, p.wpk + blk * b_stage, b_stage, fullB + 8 * sb);
-          if (++sb == NSB) { sb = 0; phb ^= 1; }
-        }
-      }
-    }
-    // Drain: every armed stage must have landed before the CTA can exit.
-    for (int i = 0; i < NSA; ++i)
-      if (armedA[i] >= 0) wait_or_flag(fullA + 8 * i, (uint32_t)armedA[i], p.err, DEV_TIMEOUT_PRODUCER);
-    for (int i = 0; i < NSB; ++i)
-      if (armedB[i] >= 0) wait_or_flag(fullB + 8 * i, (uint32_t)armedB[i], p.err, DEV_TIMEOUT_PRODUCER);
-  } else if (warp == 1 && lane == 0) {
-    // ---------------- MMA issuer ----------------
-    constexpr uint32_t idesc =
-        FP8_IN ? ptx::make_idesc(NT, 128, 0, 0) : ptx::make_idesc(NT, 128, 1, 1);
-    int sa = 0, sb = 0;
-    uint32_t pha = 0, phb = 0;
-    uint32_t accumulate = 0;
-    bool ok = true;
-    const uint32_t lboA = (uint32_t)R * 16u;
-    for (int zt = 0; zt < p.nz && ok; ++zt) {
-      for (int cg = 0; cg < p.kgroups && ok; ++cg) {
-        if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
-        ptx::tc_fence_after();
-        const uint32_t aBase = sA_u + sa * a_stage;
-        for (int yx = 0; yx < p.nyx; ++yx) {
-          if (!wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
-          ptx::tc_fence_after();
-          const uint32_t bBase = sB_u + sb * b_stage;
-          const int off = (p.nyx > 1) ? (yx / 3) * p.D + (yx % 3) : 0;
-          for (int kk = 0; kk < p.cpg / 2; ++kk) {
-            const uint64_t bdesc = ptx::smem_desc(bBase + (2 * kk) * NT * 16, NT * 16, 128);
-#pragma unroll
-            for (int i = 0; i < MSUB; ++i) {
-              const uint64_t adesc =
-                  ptx::smem_desc(aBase + (2 * kk) * lboA + (uint32_t)(i * 128 + off) * 16u, lboA, 128);
-              if (FP8_IN) ptx::mma_f8(tmem + i * NT, adesc, bdesc, idesc, accumulate);
-              else ptx::mma_f16(tmem + i * NT, adesc, bdesc, idesc, accumulate);
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- producer ----------------
+      int sa = 0, sb = 0;
+      uint32_t pha = 0, phb = 0;
+      int armedA[NSA], armedB[MAX_NSB];  // parity of each stage's last arming, -1 = never
+      for (int i = 0; i < NSA; ++i) armedA[i] = -1;
+      for (int i = 0; i < MAX_NSB; ++i) armedB[i] = -1;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+        const int64_t m0 = (t / p.ntiles) * MCTA;
+        const int nt = (int)(t % p.ntiles);
+        if (!tile_has_work(p, m0, MCTA)) continue;
+        for (int zt = 0; zt < p.nz && ok; ++zt) {
+          for (int cg = 0; cg < p.kgroups && ok; ++cg) {
+            if (!wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+            ptx::mbar_arrive_expect_tx(fullA + 8 * sa, a_stage);
+            armedA[sa] = (int)pha;
+            const uint8_t* src = p.act + (int64_t)cg * p.cpg * p.act_cs + (m0 + zt * plane) * 16;
+            for (int j = 0; j < p.cpg; ++j)
+              ptx::bulk_g2s(sA_u + sa * a_stage + j * R * 16, src + j * p.act_cs, R * 16, fullA + 8 * sa);
+            if (++sa == NSA) { sa = 0; pha ^= 1; }
+            for (int yx = 0; yx < p.nyx; ++yx) {
+              if (!wait_or_flag(emptyB + 8 * sb, phb ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+              ptx::mbar_arrive_expect_tx(fullB + 8 * sb, b_stage);
+              armedB[sb] = (int)phb;
+              const int64_t blk = (((int64_t)nt * p.nz + zt) * p.kgroups + cg) * p.nyx + yx;
+              ptx::bulk_g2s(sB_u + sb * b_stage, p.wpk + blk * b_stage, b_stage, fullB + 8 * sb);
+              if (++sb == nsb) { sb = 0; phb ^= 1; }
             }
-            accumulate = 1;
           }
-          ptx::mma_commit(emptyB + 8 * sb);
-          if (++sb == NSB) { sb = 0; phb ^= 1; }
         }
-        ptx::mma_commit(emptyA + 8 * sa);
-        if (++sa == NSA) { sa = 0; pha ^= 1; }
       }
+      // Drain: every armed stage must have landed before the CTA can exit.
+      for (int i = 0; i < NSA; ++i)
+        if (armedA[i] >= 0) wait_or_flag(fullA + 8 * i, (uint32_t)armedA[i], p.err, DEV_TIMEOUT_PRODUCER);
+      for (int i = 0; i < nsb; ++i)
+        if (armedB[i] >= 0) wait_or_flag(fullB + 8 * i, (uint32_t)armedB[i], p.err, DEV_TIMEOUT_PRODUCER);
     }
-    ptx::mma_commit(accum);  // fires once every issued MMA has completed
-  }
-  __syncwarp();
-
-  // ---------------- epilogue ----------------
-  const bool have = __all_sync(0xffffffffu, wait_or_flag(accum, 0, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0) != 0;
-  ptx::tc_fence_after();
-  if (have) {
-    const int64_t D3 = (int64_t)p.D * p.D * p.D;
-#pragma unroll 1
-    for (int i = 0; i < MSUB; ++i) {
-      const int64_t row = m0 + i * 128 + warp * 32 + lane;
-      bool valid = row < p.rows;
-      int64_t b = 0, pout = row;
-      int x = 0, y = 0, z = 0;
-      if (p.nyx > 1 && valid) {
-        b = row / D3;
-        int r = (int)(row - b * D3);
-        z = r / (p.D * p.D); y = (r / p.D) % p.D; x = r % p.D;
-        valid = x < p.Do && y < p.Do && z < p.Do;
-        pout = ((b * p.Do + z) * p.Do + y) * p.Do + x;
-      }
-#pragma unroll 1
-      for (int c0 = 0; c0 < NT; c0 += 16) {
-        float v[16];
-        ptx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * NT + c0), v);
-        if (!valid) continue;
-        const int n = n0 + c0;
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      constexpr uint32_t idesc = FP8_IN ? ptx::make_idesc(NT, 128, 0, 0) : ptx::make_idesc(NT, 128, 1, 1);
+      int sa = 0, sb = 0;
+      uint32_t pha = 0, phb = 0;
+      bool ok = true;
+      const uint32_t lboA = (uint32_t)R * 16u;
+      uint32_t j = 0;  // tiles done by this CTA
+      for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+        const int64_t m0 = (t / p.ntiles) * MCTA;
+        if (!tile_has_work(p, m0, MCTA)) continue;
+        const uint32_t buf = j & 1u, use = j >> 1;
+        if (!wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+        ptx::tc_fence_after();
+        const uint32_t dbase = tmem + buf * ACC_COLS;
+        uint32_t accumulate = 0;
+        for (int zt = 0; zt < p.nz && ok; ++zt) {
+          for (int cg = 0; cg < p.kgroups && ok; ++cg) {
+            if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+            ptx::tc_fence_after();
+            const uint32_t aBase = sA_u + sa * a_stage;
+            for (int yx = 0; yx < p.nyx; ++yx) {
+              if (!wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+              ptx::tc_fence_after();
+              const uint32_t bBase = sB_u + sb * b_stage;
+              const int off = (p.nyx > 1) ? (yx / 3) * p.D + (yx % 3) : 0;
+              for (int kk = 0; kk < p.cpg / 2; ++kk) {
+                const uint64_t bdesc = ptx::smem_desc(bBase + (2 * kk) * NT * 16, NT * 16, 128);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          float a = v[j];
-          if (FP8_IN) a = a * (p.in_scale * __ldg(p.wscale + n + j));
-          a += __ldg(p.bias + n + j);
-          if (p.relu) a = fmaxf(a, 0.0f);
-          v[j] = a;
-        }
-        if (p.out_mode == TC_OUT_F32_ROWS) {
-          float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(p.out) + row * p.cout + n);
-#pragma unroll
-          for (int h = 0; h < 4; ++h) dst[h] = make_float4(v[4 * h], v[4 * h + 1], v[4 * h + 2], v[4 * h + 3]);
-          continue;
-        }
-        if (FP8_OUT) {
-          uint4 q;
-          q.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
-          q.y = pack_e4m3x4(v[4] * p.out_qinv, v[5] * p.out_qinv, v[6] * p.out_qinv, v[7] * p.out_qinv);
-          q.z = pack_e4m3x4(v[8] * p.out_qinv, v[9] * p.out_qinv, v[10] * p.out_qinv, v[11] * p.out_qinv);
-          q.w = pack_e4m3x4(v[12] * p.out_qinv, v[13] * p.out_qinv, v[14] * p.out_qinv, v[15] * p.out_qinv);
-          int64_t chunk, prow;
-          if (p.out_mode == TC_OUT_C8_TAPS) {
-            chunk = (int64_t)((z * p.Do + y) * p.Do + x) * (p.cout / 16) + n / 16;
-            prow = b;
-          } else {
-            chunk = n / 16;
-            prow = pout;
+                for (int i = 0; i < MSUB; ++i) {
+                  const uint64_t adesc =
+                      ptx::smem_desc(aBase + (2 * kk) * lboA + (uint32_t)(i * 128 + off) * 16u, lboA, 128);
+                  if (FP8_IN) ptx::mma_f8(dbase + i * NT, adesc, bdesc, idesc, accumulate);
+                  else ptx::mma_f16(dbase + i * NT, adesc, bdesc, idesc, accumulate);
+                }
+                accumulate = 1;
+              }
+              ptx::mma_commit(emptyB + 8 * sb);
+              if (++sb == nsb) { sb = 0; phb ^= 1; }
+            }
+            ptx::mma_commit(emptyA + 8 * sa);
+            if (++sa == NSA) { sa = 0; pha ^= 1; }
           }
-          *reinterpret_cast<uint4*>(p.out + chunk * p.out_cs + prow * 16) = q;
-        } else {
+        }
+        ptx::mma_commit(accFull + 8 * buf);  // fires when this tile's MMAs are complete
+        ++j;
+      }
+      ptx::mma_commit(done);
+      wait_or_flag(done, 0, p.err, DEV_TIMEOUT_MMA);
+    }
+  } else {
+    // ---------------- epilogue (warps 2-5: TMEM lane quarter warp % 4) ----------------
+    const int q = warp & 3;
+    const int64_t D3 = (int64_t)p.D * p.D * p.D;
+    uint32_t j = 0;
+    for (int64_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
+      const int64_t m0 = (t / p.ntiles) * MCTA;
+      const int n0 = (int)(t % p.ntiles) * NT;
+      if (!tile_has_work(p, m0, MCTA)) continue;
+      const uint32_t buf = j & 1u, use = j >> 1;
+      const bool have =
+          __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0) != 0;
+      if (!have) break;
+      ptx::tc_fence_after();
+#pragma unroll 1
+      for (int i = 0; i < MSUB; ++i) {
+        const int64_t row = m0 + i * 128 + q * 32 + lane;
+        bool valid = row < p.rows;
+        int64_t b = 0, pout = row;
+        int x = 0, y = 0, z = 0;
+        if (p.nyx > 1 && valid) {
+          b = row / D3;
+          int r = (int)(row - b * D3);
+          z = r / (p.D * p.D);
+          y = (r / p.D) % p.D;
+          x = r % p.D;
+          valid = x < p.Do && y < p.Do && z < p.Do;
+          pout = ((b * p.Do + z) * p.Do + y) * p.Do + x;
+        }
+#pragma unroll 1
+        for (int c0 = 0; c0 < NT; c0 += 16) {
+          float v[16];
+          ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)(i * NT + c0), v);
+          if (!valid) continue;
+          const int n = n0 + c0;
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            uint4 q;
-            q.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
-            q.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
-            q.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
-            q.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
+          for (int e = 0; e < 16; ++e) {
+            float a = v[e];
+            if (FP8_IN) a = a * (p.in_scale * __ldg(p.wscale + n + e));
+            a += __ldg(p.bias + n + e);
+            if (p.relu) a = fmaxf(a, 0.0f);
+            v[e] = a;
+          }
+          if (p.out_mode == TC_OUT_F32_ROWS) {
+            float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(p.out) + row * p.cout + n);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) dst[h] = make_float4(v[4 * h], v[4 * h + 1], v[4 * h + 2], v[4 * h + 3]);
+            continue;
+          }
+          if (FP8_OUT) {
+            uint4 o;
+            o.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
+            o.y = pack_e4m3x4(v[4] * p.out_qinv, v[5] * p.out_qinv, v[6] * p.out_qinv, v[7] * p.out_qinv);
+            o.z = pack_e4m3x4(v[8] * p.out_qinv, v[9] * p.out_qinv, v[10] * p.out_qinv, v[11] * p.out_qinv);
+            o.w = pack_e4m3x4(v[12] * p.out_qinv, v[13] * p.out_qinv, v[14] * p.out_qinv, v[15] * p.out_qinv);
             int64_t chunk, prow;
             if (p.out_mode == TC_OUT_C8_TAPS) {
-              chunk = (int64_t)((z * p.Do + y) * p.Do + x) * (p.cout / 8) + n / 8 + h;
+              chunk = (int64_t)((z * p.Do + y) * p.Do + x) * (p.cout / 16) + n / 16;
               prow = b;
             } else {
-              chunk = n / 8 + h;
+              chunk = n / 16;
               prow = pout;
             }
-            *reinterpret_cast<uint4*>(p.out + chunk * p.out_cs + prow * 16) = q;
+            *reinterpret_cast<uint4*>(p.out + chunk * p.out_cs + prow * 16) = o;
+          } else {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              uint4 o;
+              o.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
+              o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
+              o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
+              o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
+              int64_t chunk, prow;
+              if (p.out_mode == TC_OUT_C8_TAPS) {
+                chunk = (int64_t)((z * p.Do + y) * p.Do + x) * (p.cout / 8) + n / 8 + h;
+                prow = b;
+              } else {
+                chunk = n / 8 + h;
+                prow = pout;
+              }
+              *reinterpret_cast<uint4*>(p.out + chunk * p.out_cs + prow * 16) = o;
+            }
           }
         }
       }
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(accEmpty + 8 * buf);
+      ++j;
     }
   }
   ptx::tc_fence_before();
@@ -317,21 +363,38 @@ int chunks_per_group(const TcLayer& L) {
   return chunks < 8 ? chunks : 8;
 }
 
+size_t a_stage_bytes(const TcLayer& L) { return (size_t)16 * chunks_per_group(L) * slab_rows(L); }
+
+int weight_stages(const TcLayer& L) {
+  size_t left = kSmemLimit - kSmemReserve - NSA * a_stage_bytes(L);
+  int n = (int)(left / ((size_t)L.nt * 128));
+  return n < MAX_NSB ? n : MAX_NSB;
+}
+
 size_t smem_bytes(const TcLayer& L) {
-  return (size_t)NSA * 16 * chunks_per_group(L) * slab_rows(L) + (size_t)NSB * L.nt * 128 + 256;
+  return NSA * a_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
+}
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+  }
+  return n;
 }
 
 template <int NT, int MSUB, bool FP8_IN, bool FP8_OUT>
-tdm_status launch_t(const TcLayer& L, const KParams& kp, int64_t mtiles, cudaStream_t s) {
+tdm_status launch_t(const KParams& kp, size_t smem, cudaStream_t s) {
   auto kern = tc_conv_kernel<NT, MSUB, FP8_IN, FP8_OUT>;
-  size_t smem = smem_bytes(L);
-  // Keep every tcgen05 CTA above half the SM's shared memory so that two
+  // Every tcgen05 CTA takes more than half an SM's shared memory, so two
   // TMEM-allocating CTAs never share an SM.
   size_t req = std::max<size_t>(smem, 120 * 1024);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)req);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(tc_conv_kernel)");
-  dim3 grid((unsigned)mtiles, L.cout / NT);
-  kern<<<grid, 128, req, s>>>(kp);
+  int64_t grid = std::min<int64_t>(kp.total_tiles, sm_count());
+  kern<<<(unsigned)std::max<int64_t>(grid, 1), kThreads, req, s>>>(kp);
   TDM_CHECK_LAUNCH("tc_conv_kernel");
   return TDM_OK;
 }
@@ -364,26 +427,34 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   kp.out_mode = L.out_mode;
   kp.relu = L.relu;
   kp.R = slab_rows(L);
+  kp.nsb = weight_stages(L);
   kp.err = device_error_word();
   if (!kp.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
-  TDM_REQUIRE(smem_bytes(L) <= 227 * 1024, "tc layer: shared-memory plan exceeds 227 KB");
+  TDM_REQUIRE(kp.nsb >= 2, "tc layer: shared-memory plan leaves fewer than 2 weight stages");
+  TDM_REQUIRE(smem_bytes(L) <= kSmemLimit, "tc layer: shared-memory plan exceeds 227 KB");
   TDM_REQUIRE(L.cout % L.nt == 0, "tc layer: cout must be a multiple of the N tile");
   TDM_REQUIRE((reinterpret_cast<uintptr_t>(a.act) & 15) == 0 && (a.act_cs & 15) == 0 &&
                   (reinterpret_cast<uintptr_t>(L.wpk) & 15) == 0,
               "tc layer: operands must be 16-byte aligned");
+  if (a.rows == 0) return TDM_OK;
   const int64_t mcta = (int64_t)L.msub * 128;
   const int64_t mtiles = (a.rows + mcta - 1) / mcta;
+  kp.ntiles = L.cout / L.nt;
+  kp.total_tiles = mtiles * kp.ntiles;
+  const size_t smem = smem_bytes(L);
   const bool f8i = L.fp8_in, f8o = L.fp8_out;
 #define TDM_TC_CASE(NT_, MS_)                                                                  \
   if (L.nt == NT_ && L.msub == MS_) {                                                          \
-    if (f8i && f8o) return launch_t<NT_, MS_, true, true>(L, kp, mtiles, s);                   \
-    if (f8i) return launch_t<NT_, MS_, true, false>(L, kp, mtiles, s);                         \
-    if (f8o) return launch_t<NT_, MS_, false, true>(L, kp, mtiles, s);                         \
-    return launch_t<NT_, MS_, false, false>(L, kp, mtiles, s);                                 \
+    if (f8i && f8o) return launch_t<NT_, MS_, true, true>(kp, smem, s);                        \
+    if (f8i) return launch_t<NT_, MS_, true, false>(kp, smem, s);                              \
+    if (f8o) return launch_t<NT_, MS_, false, true>(kp, smem, s);                              \
+    return launch_t<NT_, MS_, false, false>(kp, smem, s);                                      \
   }
   TDM_TC_CASE(64, 4)
-  TDM_TC_CASE(128, 4)
-  TDM_TC_CASE(256, 2)
+  TDM_TC_CASE(64, 2)
+  TDM_TC_CASE(128, 2)
+  TDM_TC_CASE(128, 1)
+  TDM_TC_CASE(256, 1)
 #undef TDM_TC_CASE
   return fail(TDM_ERR_UNSUPPORTED, "tc layer: unsupported (nt, msub) tile");
 }

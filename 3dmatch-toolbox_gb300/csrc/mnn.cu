@@ -296,7 +296,7 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
     T.nz = T.nyx = 1;
     T.kgroups = dim / 64;
     T.nt = 256;
-    T.msub = 2;
+    T.msub = 1;
     T.out_mode = TC_OUT_F32_ROWS;
     T.relu = 0;
     T.wpk = bpk;

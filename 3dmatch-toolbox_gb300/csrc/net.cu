@@ -154,9 +154,11 @@ TcLayer make_tc_layer(int l, bool use_feat) {
     L.kgroups = (l == 7 ? 27 * 512 : 512) / 64;
     L.out_mode = (l == 7 && use_feat) ? TC_OUT_C8_ROWS : TC_OUT_F32_ROWS;
   }
+  // N tile and M sub-tiles per CTA; two accumulator buffers of msub*nt TMEM
+  // columns each must fit in 512 columns.
   if (L.cout == 64) { L.nt = 64; L.msub = 4; }
-  else if (L.cout == 128) { L.nt = 128; L.msub = 4; }
-  else { L.nt = 256; L.msub = 2; }
+  else if (L.cout == 128) { L.nt = 128; L.msub = 2; }
+  else { L.nt = 256; L.msub = 1; }
   return L;
 }
 
@@ -184,6 +186,32 @@ tdm_status setup_weights(tdm_net* net) {
     return TDM_OK;
   }
   if (net->prec == TDM_BF16) {
+    // conv1 on the tensor cores: a GEMM over output positions with K = 27
+    // taps padded to 32 (im2col operand), N = 64.
+    {
+      TcLayer L{};
+      L.cin = 32;
+      L.cout = 64;
+      L.D = L.Do = 1;
+      L.nz = L.nyx = 1;
+      L.kgroups = 1;
+      L.nt = 64;
+      L.msub = 4;
+      L.out_mode = TC_OUT_C8_ROWS;
+      L.relu = 1;
+      std::vector<uint8_t> pk((size_t)4 * 64 * 16, 0);
+      for (int j = 0; j < 4; ++j)
+        for (int n = 0; n < 64; ++n)
+          for (int e = 0; e < 8; ++e) {
+            int t = 8 * j + e;
+            __nv_bfloat16 h = __float2bfloat16_rn(t < 27 ? net->hw[0][(size_t)n * 27 + t] : 0.0f);
+            std::memcpy(&pk[((size_t)j * 64 + n) * 16 + 2 * e], &h, 2);
+          }
+      st = net->upload(pk.data(), pk.size(), &L.wpk);
+      if (st != TDM_OK) return st;
+      L.bias = net->d_b[0];
+      net->tc[0] = L;
+    }
     for (int l = 1; l < 9; ++l) {
       TcLayer L = make_tc_layer(l, net->use_feat != 0);
       std::vector<uint8_t> pk;
@@ -282,6 +310,7 @@ Bf16Plan bf16_plan(const tdm_net* net, int B) {
   size_t b0 = 0, b1 = 0;
   for (int l : {1, 2, 4, 6, 8}) b0 = std::max(b0, (size_t)(l == 7 ? 1728 : chunks(l)) * P.rows_alloc[l] * 16);
   b1 = std::max(b1, (size_t)8 * ((int64_t)B * 17576 + 8) * 16);  // conv2 output (pre-pool)
+  b1 = std::max(b1, (size_t)4 * ((int64_t)B * 21952 + tc_tail_rows(net->tc[0])) * 16);  // conv1 im2col operand
   for (int l : {3, 5}) b1 = std::max(b1, (size_t)chunks(l) * P.rows_alloc[l] * 16);
   b1 = std::max(b1, (size_t)1728 * P.rows_alloc[7] * 16);  // conv7 -> conv8 flattened operand
   P.off1 = round16((int64_t)b0) + 4096;
@@ -302,10 +331,23 @@ tdm_status forward_bf16(tdm_net* net, const float* patches, int B, float* desc, 
   Bf16Plan P = bf16_plan(net, B);
   uint8_t* b0 = net->ws;
   uint8_t* b1 = net->ws + P.off1;
-  // conv1 -> chunk-planar BF16 input of conv2
+  // conv1 on tcgen05: im2col operand (in buffer 1) -> chunk-planar BF16 input of conv2
   int64_t cs = P.rows_alloc[1] * 16;
+  const int64_t rows1 = (int64_t)B * 21952;
+  const int64_t cs_i2c = (rows1 + tc_tail_rows(net->tc[0])) * 16;
   cudaEvent_t ev = net->begin(0, s);
-  tdm_status st = launch_conv1(patches, B, net->d_w1, net->d_b[0], true, b0, cs, s);
+  tdm_status st = launch_im2col_conv1(patches, B, b1, cs_i2c, s);
+  if (st) return st;
+  {
+    TcArgs a{};
+    a.act = b1;
+    a.act_cs = cs_i2c;
+    a.rows = rows1;
+    a.out = b0;
+    a.out_cs = cs;
+    a.in_scale = a.out_qinv = 1.0f;
+    st = launch_tc_layer(net->tc[0], a, s);
+  }
   net->end(ev, s);
   if (st) return st;
   if (stop == 0) return c8_response(b0, cs, B, 0, false, desc, s);
