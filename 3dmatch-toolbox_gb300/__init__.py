@@ -32,7 +32,8 @@ EXPORTS = [
     "tdm_tdf_workspace_bytes", "tdm_tdf",
     "tdm_keypoint_indices", "tdm_keypoints", "tdm_gather",
     "tdm_net_create", "tdm_net_create_from_host", "tdm_net_forward", "tdm_net_response", "tdm_net_set_max_batch",
-    "tdm_net_set_timing", "tdm_net_layer_times", "tdm_net_destroy", "tdm_write_seeded_weights",
+    "tdm_net_set_timing", "tdm_net_layer_times", "tdm_net_calibrate", "tdm_net_act_scales", "tdm_net_destroy",
+    "tdm_write_seeded_weights",
     "tdm_mnn_workspace_bytes", "tdm_match_mnn",
     "tdm_ransac_workspace_bytes", "tdm_ransac", "tdm_ransac_noalloc", "tdm_pairs_to_points",
     "tdm_tsdf_init", "tdm_depth_from_mm", "tdm_tsdf_integrate", "tdm_extract_workspace_bytes", "tdm_tsdf_extract",
@@ -109,6 +110,8 @@ def lib():
         "tdm_net_response": (i32, [P, ctypes.c_char_p, P, i32, P, P]),
         "tdm_net_set_max_batch": (i32, [P, i32]),
         "tdm_net_set_timing": (i32, [P, i32]),
+        "tdm_net_calibrate": (i32, [P, P, i32, P]),
+        "tdm_net_act_scales": (i32, [P, P]),
         "tdm_net_layer_times": (i32, [P, P, P, i32]),
         "tdm_net_destroy": (i32, [P]),
         "tdm_write_seeded_weights": (i32, [ctypes.c_char_p, u64]),
@@ -268,6 +271,15 @@ class Net:
         b = patches_dev.shape[0]
         out = torch.empty((b, D, D, D, C), dtype=torch.float32, device=patches_dev.device)
         check(lib().tdm_net_response(self.handle, name.encode(), _ptr(patches_dev), b, _ptr(out), _stream(stream)))
+        return out
+
+    def calibrate(self, patches_dev, stream=None) -> None:
+        """FP8 form: activation scales from these calibration patches."""
+        check(lib().tdm_net_calibrate(self.handle, _ptr(patches_dev), patches_dev.shape[0], _stream(stream)))
+
+    def act_scales(self):
+        out = np.zeros(9, np.float32)
+        check(lib().tdm_net_act_scales(self.handle, _ptr(out)))
         return out
 
     def set_max_batch(self, n: int) -> None:

@@ -265,7 +265,46 @@ __global__ __launch_bounds__(256) void im2col_conv1_kernel(const float* __restri
   }
 }
 
+// Same pool on the E4M3 chunk-planar layout (16 channels per 16-byte row).
+// Inputs are ReLU outputs (>= 0), whose E4M3 bytes order like the values, so
+// a byte-wise unsigned max is the max-pool.
+__global__ __launch_bounds__(256) void pool_c16_u8_kernel(const uint8_t* __restrict__ in, int64_t in_cs, int D,
+                                                          int nchunks, int64_t n_out, uint8_t* __restrict__ out,
+                                                          int64_t out_cs) {
+  int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  if (i >= n_out * nchunks) return;
+  int j = (int)(i / n_out);
+  int64_t q = i - (int64_t)j * n_out;
+  const int Do = D / 2;
+  const int64_t Do3 = (int64_t)Do * Do * Do;
+  int64_t b = q / Do3;
+  int r = (int)(q - b * Do3);
+  int z = r / (Do * Do), y = (r / Do) % Do, x = r % Do;
+  const uint8_t* src = in + (int64_t)j * in_cs;
+  uint4 best = make_uint4(0, 0, 0, 0);
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    int zz = 2 * z + (t >> 2), yy = 2 * y + ((t >> 1) & 1), xx = 2 * x + (t & 1);
+    uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (((b * D + zz) * D + yy) * D + xx) * 16));
+    best.x = __vmaxu4(best.x, v.x);
+    best.y = __vmaxu4(best.y, v.y);
+    best.z = __vmaxu4(best.z, v.z);
+    best.w = __vmaxu4(best.w, v.w);
+  }
+  *reinterpret_cast<uint4*>(out + (int64_t)j * out_cs + q * 16) = best;
+}
+
 }  // namespace
+
+tdm_status launch_pool_c16_u8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out,
+                              int64_t out_cs, cudaStream_t s) {
+  int Do = D / 2;
+  int64_t n_out = (int64_t)B * Do * Do * Do;
+  int64_t n = n_out * nchunks;
+  pool_c16_u8_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, in_cs, D, nchunks, n_out, out, out_cs);
+  TDM_CHECK_LAUNCH("pool_c16_u8_kernel");
+  return TDM_OK;
+}
 
 tdm_status launch_im2col_conv1(const float* patches, int B, uint8_t* out, int64_t out_cs, cudaStream_t s) {
   int64_t n_pos = (int64_t)B * 21952;

@@ -18,6 +18,8 @@ tdm_status launch_im2col_conv1(const float* patches, int B, uint8_t* out, int64_
 tdm_status launch_conv_f32(const float* in, int B, int D, int C, int ks, const float* w, const float* bias, int K,
                            bool relu, float* out, cudaStream_t s);
 tdm_status launch_pool_f32(const float* in, int B, int D, int C, float* out, cudaStream_t s);
+tdm_status launch_pool_c16_u8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out,
+                              int64_t out_cs, cudaStream_t s);
 tdm_status launch_pool_c8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out, int64_t out_cs,
                           cudaStream_t s);
 

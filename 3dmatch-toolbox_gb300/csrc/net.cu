@@ -19,6 +19,8 @@
 #include "internal.h"
 #include "marvin_io.h"
 
+#include <cuda_fp8.h>
+
 using namespace tdm;
 
 namespace {
@@ -55,6 +57,36 @@ __global__ void c8_to_f32_kernel(const uint8_t* __restrict__ in, int64_t cs, int
   __nv_bfloat16 v = *reinterpret_cast<const __nv_bfloat16*>(in + chunk * cs + row * 16 + (c % 8) * 2);
   out[i] = __bfloat162float(v);
 }
+// Chunk-planar E4M3 (16 channels per 16-byte row) -> float, times `scale`.
+__global__ void c16_to_f32_kernel(const uint8_t* __restrict__ in, int64_t cs, int64_t npos, int C, int taps_layout,
+                                  int ntaps, float scale, float* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npos * C) return;
+  int c = (int)(i % C);
+  int64_t p = i / C;
+  int64_t chunk, row;
+  if (taps_layout) {
+    int64_t b = p / ntaps;
+    int t = (int)(p - b * ntaps);
+    chunk = (int64_t)t * (C / 16) + c / 16;
+    row = b;
+  } else {
+    chunk = c / 16;
+    row = p;
+  }
+  __nv_fp8_e4m3 v;
+  v.__x = in[chunk * cs + row * 16 + (c % 16)];
+  out[i] = (float)v * scale;
+}
+
+// max over non-negative floats (ReLU responses) for FP8 calibration
+__global__ void amax_kernel(const float* __restrict__ x, int64_t n, unsigned int* __restrict__ out) {
+  float m = 0.0f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, x[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
 }  // namespace
 
 struct tdm_net {
@@ -65,7 +97,10 @@ struct tdm_net {
   float* d_b[9] = {};
   float* d_w1 = nullptr;  // conv1 [27][64]
   float* d_w32[9] = {};   // FP32 path: [taps*C][K]
-  TcLayer tc[9];          // tcgen05 layers (index 1..8)
+  TcLayer tc[9];          // BF16 tcgen05 layers (conv1 GEMM at 0, conv2..feat at 1..8)
+  TcLayer tc8[9];         // FP8 form: conv2 (BF16 in, E4M3 out) at 1, conv3..conv8 (E4M3 in) at 2..7
+  float act_scale[9] = {};  // FP8 form: dequantisation scale of the E4M3 input of layer l (2..7)
+  bool calibrated = false;
   std::vector<void*> allocs;
   uint8_t* ws = nullptr;
   size_t ws_bytes = 0;
@@ -185,7 +220,7 @@ tdm_status setup_weights(tdm_net* net) {
     }
     return TDM_OK;
   }
-  if (net->prec == TDM_BF16) {
+  if (net->prec == TDM_BF16 || net->prec == TDM_FP8) {
     // conv1 on the tensor cores: a GEMM over output positions with K = 27
     // taps padded to 32 (im2col operand), N = 64.
     {
@@ -223,9 +258,32 @@ tdm_status setup_weights(tdm_net* net) {
       L.wscale = nullptr;
       net->tc[l] = L;
     }
+    if (net->prec == TDM_BF16) return TDM_OK;
+    // FP8 form: conv2 keeps BF16 operands but writes E4M3; conv3..conv8 take
+    // E4M3 operands with per-output-channel weight scales.
+    net->tc8[1] = net->tc[1];
+    net->tc8[1].fp8_out = true;
+    for (int l = 2; l < 8; ++l) {
+      TcLayer L = make_tc_layer(l, net->use_feat != 0);
+      L.fp8_in = true;
+      L.fp8_out = l < 7;
+      const int k_total = l <= 6 ? kCin[l] : 27 * 512;  // K elements per tap (conv) or in total (conv8)
+      const int chunks = k_total / 16;
+      L.kgroups = chunks < 8 ? 1 : chunks / 8;
+      std::vector<uint8_t> pk;
+      std::vector<float> sc;
+      pack_tc_weights(L, net->hw[l].data(), l == 7 ? 27 : 1, &pk, &sc);
+      st = net->upload(pk.data(), pk.size(), &L.wpk);
+      if (st != TDM_OK) return st;
+      st = net->upload(sc.data(), sc.size(), &L.wscale);
+      if (st != TDM_OK) return st;
+      L.bias = net->d_b[l];
+      net->tc8[l] = L;
+    }
+    net->tc8[8] = net->tc[8];
     return TDM_OK;
   }
-  return fail(TDM_ERR_UNSUPPORTED, "precision not available for the net yet");
+  return fail(TDM_ERR_UNSUPPORTED, "unknown precision");
 }
 
 tdm_status create_common(tdm_net* net, tdm_precision prec, int32_t use_feat) {
@@ -327,7 +385,22 @@ tdm_status c8_response(const uint8_t* src, int64_t cs, int B, int id, bool taps,
   return TDM_OK;
 }
 
-tdm_status forward_bf16(tdm_net* net, const float* patches, int B, float* desc, int stop, cudaStream_t s) {
+tdm_status c16_response(const uint8_t* src, int64_t cs, int B, int id, bool taps, float scale, float* out,
+                        cudaStream_t s) {
+  int D, C;
+  response_shape(id, &D, &C);
+  int64_t npos = (int64_t)B * D * D * D;
+  c16_to_f32_kernel<<<(unsigned)((npos * C + 255) / 256), 256, 0, s>>>(src, cs, npos, C, taps ? 1 : 0, D * D * D,
+                                                                        scale, out);
+  TDM_CHECK_LAUNCH("c16_to_f32_kernel");
+  return TDM_OK;
+}
+
+// Tensor-core forward of one chunk.  BF16 form: BF16 activations between all
+// layers.  FP8 form (fp8 = true): conv2 writes E4M3, conv3..conv7 read and
+// write E4M3 with per-tensor activation scales, conv8 reads E4M3 and writes
+// BF16 for feat.
+tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, int stop, bool fp8, cudaStream_t s) {
   Bf16Plan P = bf16_plan(net, B);
   uint8_t* b0 = net->ws;
   uint8_t* b1 = net->ws + P.off1;
@@ -355,15 +428,16 @@ tdm_status forward_bf16(tdm_net* net, const float* patches, int B, float* desc, 
   int64_t cur_cs = cs;
   for (int l = 1; l < 9; ++l) {
     if (l == 8 && !net->use_feat) break;
-    const TcLayer& L = net->tc[l];
+    const bool l_fp8 = fp8 && l <= 7;
+    const TcLayer& L = l_fp8 ? net->tc8[l] : net->tc[l];
     bool last = (l == 8) || (l == 7 && !net->use_feat);
     uint8_t* dst = (cur == b0) ? b1 : b0;
     TcArgs a{};
     a.act = cur;
     a.act_cs = cur_cs;
     a.rows = P.rows[l];
-    a.in_scale = 1.0f;
-    a.out_qinv = 1.0f;
+    a.in_scale = L.fp8_in ? net->act_scale[l] : 1.0f;
+    a.out_qinv = L.fp8_out ? 1.0f / net->act_scale[l + 1] : 1.0f;
     int64_t out_cs = 0;
     if (last) {
       a.out = reinterpret_cast<uint8_t*>(desc);
@@ -382,14 +456,22 @@ tdm_status forward_bf16(tdm_net* net, const float* patches, int B, float* desc, 
     net->end(ev, s);
     if (st) return st;
     if (last) break;
-    if (stop == l) return c8_response(dst, out_cs, B, l, L.out_mode == TC_OUT_C8_TAPS, desc, s);
+    if (stop == l) {
+      const bool taps = L.out_mode == TC_OUT_C8_TAPS;
+      if (L.fp8_out) return c16_response(dst, out_cs, B, l, taps, net->act_scale[l + 1], desc, s);
+      return c8_response(dst, out_cs, B, l, taps, desc, s);
+    }
     if (l == 1) {  // pool 26^3 -> 13^3 back into buffer 0 as conv3's input
       int64_t pcs = P.rows_alloc[2] * 16;
       ev = net->begin(9, s);
-      st = launch_pool_c8(dst, out_cs, B, 26, 8, cur, pcs, s);
+      st = fp8 ? launch_pool_c16_u8(dst, out_cs, B, 26, 4, cur, pcs, s)
+               : launch_pool_c8(dst, out_cs, B, 26, 8, cur, pcs, s);
       net->end(ev, s);
       if (st) return st;
-      if (stop == kPool) return c8_response(cur, pcs, B, kPool, false, desc, s);
+      if (stop == kPool) {
+        if (fp8) return c16_response(cur, pcs, B, kPool, false, net->act_scale[2], desc, s);
+        return c8_response(cur, pcs, B, kPool, false, desc, s);
+      }
       cur_cs = pcs;
       continue;
     }
@@ -464,9 +546,14 @@ extern "C" tdm_status tdm_net_create(const char* path, tdm_precision prec, int32
   return tdm_net_create_from_host(w, b, prec, use_feat, out);
 }
 
-static tdm_status net_run(tdm_net* net, const float* patches, int32_t b, float* out, int stop, tdm_stream s) {
+// form: the precision to run (an FP8 net can also run its BF16 form, which
+// calibration uses).
+static tdm_status net_run(tdm_net* net, const float* patches, int32_t b, float* out, int stop, tdm_stream s,
+                          tdm_precision form) {
   if (b == 0) return TDM_OK;
   TDM_REQUIRE(patches && out, "tdm_net_forward: null pointer");
+  TDM_REQUIRE(form != TDM_FP8 || net->calibrated,
+              "FP8 net has no activation scales yet: call tdm_net_calibrate first");
   const int chunk = std::min<int>(b, net->max_batch);
   size_t need = net->prec == TDM_FP32 ? f32_ws_bytes(chunk) : bf16_plan(net, chunk).total;
   tdm_status st = ensure_ws(net, need);
@@ -481,7 +568,8 @@ static tdm_status net_run(tdm_net* net, const float* patches, int32_t b, float* 
     int n = std::min(chunk, b - i);
     const float* p = patches + (size_t)i * 27000;
     float* d = out + (size_t)i * per;
-    st = net->prec == TDM_FP32 ? forward_f32(net, p, n, d, stop, s) : forward_bf16(net, p, n, d, stop, s);
+    st = form == TDM_FP32 ? forward_f32(net, p, n, d, stop, s)
+                          : forward_tc(net, p, n, d, stop, form == TDM_FP8, s);
     if (st) return st;
   }
   return TDM_OK;
@@ -489,7 +577,7 @@ static tdm_status net_run(tdm_net* net, const float* patches, int32_t b, float* 
 
 extern "C" tdm_status tdm_net_forward(tdm_net* net, const float* patches, int32_t b, float* desc, tdm_stream s) {
   TDM_REQUIRE(net && b >= 0, "tdm_net_forward: bad arguments");
-  return net_run(net, patches, b, desc, -1, s);
+  return net_run(net, patches, b, desc, -1, s, net->prec);
 }
 
 extern "C" tdm_status tdm_net_response(tdm_net* net, const char* name, const float* patches, int32_t b, float* out,
@@ -502,7 +590,57 @@ extern "C" tdm_status tdm_net_response(tdm_net* net, const char* name, const flo
   if (n == "pool1") id = kPool;
   TDM_REQUIRE(id != -2, "tdm_net_response: unknown response name");
   TDM_REQUIRE(!(id == 8 && !net->use_feat), "tdm_net_response: net built without feat");
-  return net_run(net, patches, b, out, id, s);
+  return net_run(net, patches, b, out, id, s, net->prec);
+}
+
+extern "C" tdm_status tdm_net_calibrate(tdm_net* net, const float* patches, int32_t b, tdm_stream s) {
+  TDM_REQUIRE(net && patches && b > 0, "tdm_net_calibrate: bad arguments");
+  if (net->prec != TDM_FP8) return TDM_OK;
+  // Largest activation of conv2..conv7 over the calibration patches in the
+  // BF16 form; the E4M3 scale maps it to 448 (the largest finite E4M3).
+  int64_t maxn = (int64_t)b * 26 * 26 * 26 * 64;
+  float* buf = nullptr;
+  unsigned int* amax = nullptr;
+  TDM_CHECK_CUDA(cudaMalloc(&buf, sizeof(float) * maxn));
+  cudaError_t e = cudaMalloc(&amax, sizeof(unsigned int) * 8);
+  if (e != cudaSuccess) {
+    cudaFree(buf);
+    return cuda_status(e, "calibration buffer");
+  }
+  tdm_status st = TDM_OK;
+  for (int l = 1; l <= 6 && st == TDM_OK; ++l) {
+    st = net_run(net, patches, b, buf, l, s, TDM_BF16);
+    if (st) break;
+    int D, C;
+    response_shape(l, &D, &C);
+    int64_t n = (int64_t)b * D * D * D * C;
+    if (cudaMemsetAsync(amax + l, 0, sizeof(unsigned int), s) != cudaSuccess) { st = TDM_ERR_DEVICE; break; }
+    amax_kernel<<<1216, 256, 0, s>>>(buf, n, amax + l);
+    if (cudaGetLastError() != cudaSuccess) st = fail(TDM_ERR_DEVICE, "amax_kernel launch failed");
+    note_launches(1);
+  }
+  unsigned int h[8] = {};
+  if (st == TDM_OK) {
+    e = cudaMemcpyAsync(h, amax, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "calibration readback");
+  }
+  cudaFree(buf);
+  cudaFree(amax);
+  if (st) return st;
+  for (int l = 1; l <= 6; ++l) {
+    float m;
+    std::memcpy(&m, &h[l], 4);
+    net->act_scale[l + 1] = (m > 0.0f ? m : 1.0f) / 448.0f;
+  }
+  net->calibrated = true;
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_net_act_scales(tdm_net* net, float* scales) {
+  TDM_REQUIRE(net && scales, "tdm_net_act_scales: null pointer");
+  for (int l = 0; l < 9; ++l) scales[l] = net->act_scale[l];
+  return TDM_OK;
 }
 
 extern "C" tdm_status tdm_net_set_max_batch(tdm_net* net, int32_t max_batch) {

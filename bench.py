@@ -43,7 +43,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp8", "fp32"])
+    ap.add_argument("--fp8-steps", type=int, default=5)
     ap.add_argument("--keypoints", type=int, default=1000)
     ap.add_argument("--points", type=int, default=150_000)
     ap.add_argument("--ransac-iters", type=int, default=100_000)
@@ -238,10 +239,27 @@ def run_ours(args, rank, world, local):
     wfile = os.path.join(tempfile.gettempdir(), "tdm_bench_weights_%d.marvin" % os.getpid())
     tdm.write_seeded_weights(wfile, 20260000)
 
+    calib = None
+
+    def calibration_patches():
+        # seeded calibration batch: 256 patches of a separate synthetic fragment
+        cp = synth.fragment(20269999, n_points=args.points)
+        pd = torch.from_numpy(cp).to(dev)
+        g = tdm.grid_from_points_host(cp)
+        t = tdm.tdf(pd, g)
+        _, kg = tdm.keypoints(pd, tdm.keypoint_indices(20269999, cp.shape[0], 256, device=dev), g)
+        return tdm.gather(t, g, kg)
+
     def make(prec):
+        nonlocal calib
         net = tdm.Net(marvin_path=wfile, precision=prec)
+        if prec == "fp8":
+            if calib is None:
+                calib = calibration_patches()
+            net.calibrate(calib)
         pipe = tdm.Pipeline(net, max_keypoints=k, max_points=max(p[0].shape[0] for p in pairs) + 16,
-                            max_voxels=80_000_000, match_precision=prec, ransac_seed=20260000,
+                            max_voxels=80_000_000, match_precision="bf16" if prec == "fp8" else prec,
+                            ransac_seed=20260000,
                             ransac_iters=args.ransac_iters)
         return net, pipe
 
@@ -305,6 +323,22 @@ def run_ours(args, rank, world, local):
         fp32 = world * args.fp32_steps / (ms32 / 1000.0)
         pipe32.close()
         net32.close()
+    # FP8 form (E4M3 conv3..conv8) on the same GPU
+    fp8 = None
+    if prec != "fp8" and args.fp8_steps > 0:
+        net8, pipe8 = make("fp8")
+        pipe8.register(*dpairs[0], seed=1, k=k)
+        ms8, _, _ = timed(pipe8, args.fp8_steps)
+        fp8 = world * args.fp8_steps / (ms8 / 1000.0)
+        pipe8.close()
+        net8.close()
+    # per-pair latency of the headline form (one pair per call, synchronous)
+    lat = []
+    for s_ in range(args.steps):
+        a, b = dpairs[s_ % len(dpairs)]
+        t0 = time.perf_counter()
+        pipe.register(a, b, seed=2000 + s_, k=k)
+        lat.append((time.perf_counter() - t0) * 1000.0)
     # roofline of the dominant kernel: conv2 on tcgen05 (useful FLOPs per launch / event time)
     conv2_ms, conv2_n = lt["conv2"]
     peaks, peak_kind = load_peaks()
@@ -336,7 +370,10 @@ def run_ours(args, rank, world, local):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "working set > L2 (net activations %.1f GB per step)" % (2 * k * 5.1e6 / 1e9),
                        "fp32_pairs_per_s": fp32,
+                       "fp8_pairs_per_s": fp8,
                        "bf16_over_fp32": (value / fp32) if fp32 else None,
+                       "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                                      "n": len(lat)},
                        "net_tflops_useful": 2 * k * NET_FLOP_PER_PATCH / (ms_step / 1000.0) / 1e12,
                        "layer_ms_per_launch": layer_ms,
                        "last_result": {"matches": res.n_matches, "inliers": res.n_inliers} if res else None},

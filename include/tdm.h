@@ -113,6 +113,12 @@ tdm_status tdm_net_forward(tdm_net* net, const float* patches_dev, int32_t b, fl
  * writes it as float, channels-last [b][D][D][D][C] (Marvin keeps NCDHW). */
 tdm_status tdm_net_response(tdm_net* net, const char* name, const float* patches_dev, int32_t b, float* out_dev,
                             tdm_stream s);
+/* FP8 form only (no-op otherwise): sets the per-tensor E4M3 activation scales
+ * of conv3..conv8's inputs from the largest activations of b calibration
+ * patches in the BF16 form (scale = max / 448).  Required before the first
+ * FP8 forward.  tdm_net_act_scales returns the 9 scales (index = layer). */
+tdm_status tdm_net_calibrate(tdm_net* net, const float* patches_dev, int32_t b, tdm_stream s);
+tdm_status tdm_net_act_scales(tdm_net* net, float* scales);
 /* Patches per internal chunk (bounds the activation workspace; default 2048). */
 tdm_status tdm_net_set_max_batch(tdm_net* net, int32_t max_batch);
 /* Per-layer device time, the analogue of Marvin's debug_mode tic/toc

@@ -120,3 +120,43 @@ def test_marvin_file_path(tdm, oracle, patches, tmp_path):
     got = net.forward(patches[:3]).cpu().numpy()
     want = oracle.net_forward(patches[:3].cpu().numpy(), w)
     assert rel_l2(got, want) <= 1e-4
+
+
+FP8_RESPONSES = ["conv2", "pool1", "conv3", "conv4", "conv5", "conv6", "conv7", "conv8", "feat"]
+
+
+@pytest.fixture(scope="module")
+def fp8_net(tdm, weights, patches):
+    net = tdm.Net(weights, precision="fp8")
+    net.calibrate(patches[:4].contiguous())  # the oracle responses cover these four
+    return net
+
+
+def test_fp8_requires_calibration(tdm, weights, patches):
+    net = tdm.Net(weights, precision="fp8")
+    with pytest.raises(tdm.TdmError, match="calibrate"):
+        net.forward(patches)
+
+
+def test_fp8_scales(fp8_net, oracle_resp):
+    sc = fp8_net.act_scales()
+    # scale of layer l's input = max of layer l-1's response / 448 (responses of the BF16 form)
+    for l, name in zip(range(2, 8), ["conv2", "conv3", "conv4", "conv5", "conv6", "conv7"]):
+        assert sc[l] > 0
+        assert abs(sc[l] * 448 / oracle_resp[name].max() - 1) < 0.05, name
+
+
+@pytest.mark.parametrize("name", FP8_RESPONSES)
+def test_fp8_responses(fp8_net, patches, oracle_resp, name):
+    got = fp8_net.response(name, patches[:4]).cpu().numpy()
+    err = rel_l2(got, oracle_resp[name])
+    assert err <= 0.1, (name, err)  # E4M3 keeps 3 mantissa bits
+
+
+def test_fp8_descriptors(tdm, oracle, fp8_net, weights, patches):
+    got = fp8_net.forward(patches).cpu().numpy()
+    want64 = oracle.net_forward(patches.cpu().numpy(), weights, f64=True)
+    err = rel_l2(got, want64)
+    print("fp8 descriptor rel-L2 vs FP64:", err)
+    assert err <= 0.1
+    tdm.device_status()
