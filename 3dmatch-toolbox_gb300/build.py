@@ -29,6 +29,9 @@ LIB_PATH = os.path.join(LIB, "libtdm.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I" + INC, "-I" + CSRC] + ARCH
+# Extra flags for diagnostic builds (e.g. -DTDM_WAIT_STATS); objects built
+# with different flags are not mixed (the flags are part of the stamp).
+EXTRA = os.environ.get("TDM_EXTRA_NVCC_FLAGS", "").split()
 # Translation units whose float results are compared bit for bit with the
 # CPU restatement: no multiply-add contraction on the device either.
 NO_FMAD = {"ransac.cu", "tsdf.cu"}
@@ -69,7 +72,7 @@ def _compile(src: str, hdrs) -> str:
         return obj
     tmp = obj + ".tmp%d" % os.getpid()
     if src.endswith(".cu"):
-        flags = list(NVCC_FLAGS)
+        flags = list(NVCC_FLAGS) + EXTRA
         if name in NO_FMAD:
             flags.append("-fmad=false")
         _run([_nvcc()] + flags + ["-c", src, "-o", tmp])
@@ -82,7 +85,7 @@ def _compile(src: str, hdrs) -> str:
 def _arch_guard() -> None:
     """Objects built on another host architecture are discarded."""
     stamp = os.path.join(OBJ, "ARCH")
-    mach = platform.machine()
+    mach = platform.machine() + " " + " ".join(EXTRA)
     old = open(stamp).read().strip() if os.path.exists(stamp) else None
     if old != mach:
         for d in (OBJ, LIB, BIN):

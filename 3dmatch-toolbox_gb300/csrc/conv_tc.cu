@@ -87,6 +87,22 @@ __device__ __forceinline__ bool wait_or_flag(uint32_t bar, uint32_t parity, int*
   }
 }
 
+#ifdef TDM_WAIT_STATS
+// Diagnostic build only: cycles spent in each kind of wait, summed over CTAs.
+// slots: 0 MMA<-accEmpty, 1 MMA<-fullA, 2 MMA<-fullB, 3 producer<-emptyA,
+//        4 producer<-emptyB, 5 epilogue<-accFull, 6 MMA loop total, 7 producer loop total
+__device__ unsigned long long g_wait_stats[8];
+#define TDM_TIMED_WAIT(slot, expr)                                           \
+  ([&]() {                                                                   \
+    long long _c0 = clock64();                                               \
+    bool _r = (expr);                                                        \
+    atomicAdd(&g_wait_stats[slot], (unsigned long long)(clock64() - _c0));   \
+    return _r;                                                               \
+  }())
+#else
+#define TDM_TIMED_WAIT(slot, expr) (expr)
+#endif
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
@@ -165,6 +181,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
   if (warp == 0) {
     if (lane == 0) {
       // ---------------- producer ----------------
+#ifdef TDM_WAIT_STATS
+      const long long t_loop0 = clock64();
+#endif
       int sa = 0, sb = 0;
       uint32_t pha = 0, phb = 0;
       int armedA[NSA], armedB[MAX_NSB];  // parity of each stage's last arming, -1 = never
@@ -177,7 +196,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
         if (!tile_has_work(p, m0, MCTA)) continue;
         for (int zt = 0; zt < p.nz && ok; ++zt) {
           for (int cg = 0; cg < p.kgroups && ok; ++cg) {
-            if (!wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+            if (!TDM_TIMED_WAIT(3, wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
             ptx::mbar_arrive_expect_tx(fullA + 8 * sa, a_stage);
             armedA[sa] = (int)pha;
             const uint8_t* src = p.act + (int64_t)cg * p.cpg * p.act_cs + (m0 + zt * plane) * 16;
@@ -185,7 +204,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
               ptx::bulk_g2s(sA_u + sa * a_stage + j * R * 16, src + j * p.act_cs, R * 16, fullA + 8 * sa);
             if (++sa == NSA) { sa = 0; pha ^= 1; }
             for (int yx = 0; yx < p.nyx; ++yx) {
-              if (!wait_or_flag(emptyB + 8 * sb, phb ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+              if (!TDM_TIMED_WAIT(4, wait_or_flag(emptyB + 8 * sb, phb ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
               ptx::mbar_arrive_expect_tx(fullB + 8 * sb, b_stage);
               armedB[sb] = (int)phb;
               const int64_t blk = (((int64_t)nt * p.nz + zt) * p.kgroups + cg) * p.nyx + yx;
@@ -195,6 +214,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
           }
         }
       }
+#ifdef TDM_WAIT_STATS
+      atomicAdd(&g_wait_stats[7], (unsigned long long)(clock64() - t_loop0));
+#endif
       // Drain: every armed stage must have landed before the CTA can exit.
       for (int i = 0; i < NSA; ++i)
         if (armedA[i] >= 0) wait_or_flag(fullA + 8 * i, (uint32_t)armedA[i], p.err, DEV_TIMEOUT_PRODUCER);
@@ -204,6 +226,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
+#ifdef TDM_WAIT_STATS
+      const long long t_loop0 = clock64();
+#endif
       constexpr uint32_t idesc = FP8_IN ? ptx::make_idesc(NT, 128, 0, 0) : ptx::make_idesc(NT, 128, 1, 1);
       int sa = 0, sb = 0;
       uint32_t pha = 0, phb = 0;
@@ -214,17 +239,17 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
         const int64_t m0 = (t / p.ntiles) * MCTA;
         if (!tile_has_work(p, m0, MCTA)) continue;
         const uint32_t buf = j & 1u, use = j >> 1;
-        if (!wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+        if (!TDM_TIMED_WAIT(0, wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
         ptx::tc_fence_after();
         const uint32_t dbase = tmem + buf * ACC_COLS;
         uint32_t accumulate = 0;
         for (int zt = 0; zt < p.nz && ok; ++zt) {
           for (int cg = 0; cg < p.kgroups && ok; ++cg) {
-            if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+            if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
             ptx::tc_fence_after();
             const uint32_t aBase = sA_u + sa * a_stage;
             for (int yx = 0; yx < p.nyx; ++yx) {
-              if (!wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+              if (!TDM_TIMED_WAIT(2, wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
               ptx::tc_fence_after();
               const uint32_t bBase = sB_u + sb * b_stage;
               const int off = (p.nyx > 1) ? (yx / 3) * p.D + (yx % 3) : 0;
@@ -251,6 +276,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
       }
       ptx::mma_commit(done);
       wait_or_flag(done, 0, p.err, DEV_TIMEOUT_MMA);
+#ifdef TDM_WAIT_STATS
+      atomicAdd(&g_wait_stats[6], (unsigned long long)(clock64() - t_loop0));
+#endif
     }
   } else {
     // ---------------- epilogue (warps 2-5: TMEM lane quarter warp % 4) ----------------
@@ -263,7 +291,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
       if (!tile_has_work(p, m0, MCTA)) continue;
       const uint32_t buf = j & 1u, use = j >> 1;
       const bool have =
-          __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0) != 0;
+          __all_sync(0xffffffffu,
+                     TDM_TIMED_WAIT(5, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE)) ? 1 : 0) != 0;
       if (!have) break;
       ptx::tc_fence_after();
 #pragma unroll 1
@@ -400,6 +429,19 @@ tdm_status launch_t(const KParams& kp, size_t smem, cudaStream_t s) {
 }
 
 }  // namespace
+
+#ifdef TDM_WAIT_STATS
+}  // namespace tdm
+extern "C" int tdm_debug_wait_stats(unsigned long long* out, int reset) {
+  if (cudaMemcpyFromSymbol(out, tdm::g_wait_stats, sizeof(unsigned long long) * 8) != cudaSuccess) return 1;
+  if (reset) {
+    unsigned long long z[8] = {};
+    if (cudaMemcpyToSymbol(tdm::g_wait_stats, z, sizeof(z)) != cudaSuccess) return 1;
+  }
+  return 0;
+}
+namespace tdm {
+#endif
 
 int64_t tc_tail_rows(const TcLayer& L) {
   return (int64_t)(L.nz > 1 ? 2 * L.D * L.D : 0) + slab_rows(L) + 8;

@@ -2,8 +2,8 @@
 //
 // Replaces core/demo.cu:97-218.  The reference's ComputeTDF (core/demo.cu:22-57)
 // scans an 11^3 cube per empty voxel (1,331 occupancy reads).  Here the same
-// value comes from an exact separable windowed squared distance computed in
-// shared-memory tiles:
+// value comes from an exact separable windowed squared distance (an in-plane
+// pass per z-plane in shared memory, then a pass along z):
 //   g1 = min_{|dx|<=r, occ} dx^2,  g2 = min_{|dy|<=r} dy^2 + g1,  g3 = min_{|dz|<=r} dz^2 + g2
 // which is the minimum of dx^2+dy^2+dz^2 over the occupied voxels of the cube.
 // Because sqrtf, /r and 1-x are monotone, 1 - sqrtf(g3)/r equals the
@@ -20,7 +20,6 @@ using namespace tdm;
 
 namespace {
 
-constexpr uint16_t kNone = 0xFFFF;
 
 __device__ __forceinline__ int float_to_ordered(float f) {
   int i = __float_as_int(f);
@@ -79,68 +78,77 @@ __global__ __launch_bounds__(256) void occupancy_kernel(const float* __restrict_
   occ[((int64_t)gz * dy + gy) * dx + gx] = 1;
 }
 
-constexpr int TX = 32, TY = 8, TZ = 8;
+// Pass A, one z-plane per block row: g2[z][y][x] = min over the in-plane
+// (2r+1)^2 window of dx^2 + dy^2 over occupied voxels (kNone8 = none).  The
+// occupancy rows of a 16-row band (plus halo) are staged in shared memory,
+// scanned along x, then along y; g2 is written as bytes (it stays in L2).
+constexpr int PA_TY = 16, PA_TX = 512;
+constexpr uint8_t kNone8 = 0xFF;
 
 template <int R>
-__global__ __launch_bounds__(256) void tdf_tile_kernel(const uint8_t* __restrict__ occ, int dx, int dy, int dz,
-                                                       float* __restrict__ tdf) {
-  constexpr int IX = TX + 2 * R, IY = TY + 2 * R, IZ = TZ + 2 * R;
-  __shared__ uint8_t s_occ[IZ][IY][IX];
-  __shared__ uint16_t s_g1[IZ][IY][TX];
-  __shared__ uint16_t s_g2[IZ][TY][TX];
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-  const int tid = threadIdx.x;
-
-  for (int i = tid; i < IX * IY * IZ; i += 256) {
-    int lx = i % IX, ly = (i / IX) % IY, lz = i / (IX * IY);
-    int gx = x0 - R + lx, gy = y0 - R + ly, gz = z0 - R + lz;
-    uint8_t v = 0;
-    if (gx >= 0 && gy >= 0 && gz >= 0 && gx < dx && gy < dy && gz < dz) v = occ[((int64_t)gz * dy + gy) * dx + gx];
-    s_occ[lz][ly][lx] = v;
-  }
-  __syncthreads();
-  for (int i = tid; i < TX * IY * IZ; i += 256) {  // along x
-    int lx = i % TX, ly = (i / TX) % IY, lz = i / (TX * IY);
-    int best = kNone;
-#pragma unroll
-    for (int d = -R; d <= R; ++d)
-      if (s_occ[lz][ly][lx + R + d]) best = min(best, d * d);
-    s_g1[lz][ly][lx] = (uint16_t)best;
-  }
-  __syncthreads();
-  for (int i = tid; i < TX * TY * IZ; i += 256) {  // along y
-    int lx = i % TX, ly = (i / TX) % TY, lz = i / (TX * TY);
-    int best = kNone;
-#pragma unroll
-    for (int d = -R; d <= R; ++d) {
-      int v = s_g1[lz][ly + R + d][lx];
-      if (v != kNone) best = min(best, v + d * d);
+__global__ __launch_bounds__(256) void tdf_plane_kernel(const uint8_t* __restrict__ occ, int dx, int dy,
+                                                        uint8_t* __restrict__ g2) {
+  __shared__ uint8_t s_occ[PA_TY + 2 * R][PA_TX + 2 * R];
+  __shared__ uint8_t s_g1[PA_TY + 2 * R][PA_TX];
+  const int x0 = blockIdx.x * PA_TX, y0 = blockIdx.y * PA_TY, z = blockIdx.z;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t plane = (int64_t)dx * dy;
+  const uint8_t* src = occ + (int64_t)z * plane;
+  const int tx = min(PA_TX, dx - x0);
+  for (int ly = warp; ly < PA_TY + 2 * R; ly += 8) {
+    const int gy = y0 - R + ly;
+    const bool row_in = gy >= 0 && gy < dy;
+    for (int lx = lane; lx < tx + 2 * R; lx += 32) {
+      const int gx = x0 - R + lx;
+      s_occ[ly][lx] = (row_in && gx >= 0 && gx < dx) ? src[(int64_t)gy * dx + gx] : 0;
     }
-    s_g2[lz][ly][lx] = (uint16_t)best;
   }
   __syncthreads();
-  for (int i = tid; i < TX * TY * TZ; i += 256) {  // along z, then the TDF value
-    int lx = i % TX, ly = (i / TX) % TY, lz = i / (TX * TY);
-    int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
-    if (gx >= dx || gy >= dy || gz >= dz) continue;
-    float out;
-    if (s_occ[lz + R][ly + R][lx + R]) {
-      out = 1.0f;
-    } else {
-      int best = kNone;
+  for (int ly = warp; ly < PA_TY + 2 * R; ly += 8)
+    for (int lx = lane; lx < tx; lx += 32) {
+      int best = kNone8;
+#pragma unroll
+      for (int d = -R; d <= R; ++d)
+        if (s_occ[ly][lx + R + d]) best = min(best, d * d);
+      s_g1[ly][lx] = (uint8_t)best;
+    }
+  __syncthreads();
+  const int ny = min(PA_TY, dy - y0);
+  uint8_t* dst = g2 + (int64_t)z * plane;
+  for (int ly = warp; ly < ny; ly += 8)
+    for (int lx = lane; lx < tx; lx += 32) {
+      int best = kNone8;
 #pragma unroll
       for (int d = -R; d <= R; ++d) {
-        int v = s_g2[lz + R + d][ly][lx];
-        if (v != kNone) best = min(best, v + d * d);
+        int v = s_g1[ly + R + d][lx];
+        if (v != kNone8) best = min(best, v + d * d);
       }
-      out = 0.0f;
-      if (best != kNone) {
-        float v = __fsub_rn(1.0f, __fdiv_rn(__fsqrt_rn((float)best), (float)R));
-        out = v > 0.0f ? v : 0.0f;
-      }
+      dst[(int64_t)(y0 + ly) * dx + x0 + lx] = (uint8_t)best;
     }
-    tdf[((int64_t)gz * dy + gy) * dx + gx] = out;
+}
+
+// Pass B: along z, then the TDF value.  Distance 0 is the voxel's own
+// occupancy, so 1 - sqrtf(0)/r = 1 reproduces the reference's "occupied -> 1".
+template <int R>
+__global__ __launch_bounds__(256) void tdf_z_kernel(const uint8_t* __restrict__ g2, int64_t plane, int dz,
+                                                    float* __restrict__ tdf) {
+  const int64_t v = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  if (v >= plane * dz) return;
+  const int z = (int)(v / plane);
+  int best = 0xFFFF;
+#pragma unroll
+  for (int d = -R; d <= R; ++d) {
+    const int zz = z + d;
+    if (zz < 0 || zz >= dz) continue;
+    const int g = __ldg(g2 + v + (int64_t)d * plane);
+    if (g != kNone8) best = min(best, g + d * d);
   }
+  float out = 0.0f;
+  if (best != 0xFFFF) {
+    const float val = __fsub_rn(1.0f, __fdiv_rn(__fsqrt_rn((float)best), (float)R));
+    out = val > 0.0f ? val : 0.0f;
+  }
+  tdf[v] = out;
 }
 
 // The reference decodes voxel_idx through float32 (core/demo.cu:32-34); above
@@ -236,9 +244,12 @@ __global__ __launch_bounds__(256) void gather_kernel(const float* __restrict__ t
 }
 
 template <int R>
-void launch_tdf_tile(const uint8_t* occ, const tdm_grid* g, float* tdf, cudaStream_t s) {
-  dim3 grid((g->dim[0] + TX - 1) / TX, (g->dim[1] + TY - 1) / TY, (g->dim[2] + TZ - 1) / TZ);
-  tdf_tile_kernel<R><<<grid, 256, 0, s>>>(occ, g->dim[0], g->dim[1], g->dim[2], tdf);
+void launch_tdf(const uint8_t* occ, uint8_t* g2, const tdm_grid* g, float* tdf, cudaStream_t s) {
+  dim3 ga((g->dim[0] + PA_TX - 1) / PA_TX, (g->dim[1] + PA_TY - 1) / PA_TY, g->dim[2]);
+  tdf_plane_kernel<R><<<ga, 256, 0, s>>>(occ, g->dim[0], g->dim[1], g2);
+  const int64_t plane = (int64_t)g->dim[0] * g->dim[1];
+  const int64_t V = plane * g->dim[2];
+  tdf_z_kernel<R><<<(unsigned)((V + 255) / 256), 256, 0, s>>>(g2, plane, g->dim[2], tdf);
 }
 
 int search_radius(const tdm_grid* g) { return (int)roundf(g->trunc_margin / g->voxel_size); }
@@ -270,35 +281,38 @@ extern "C" tdm_status tdm_grid_from_points(const float* pts, int32_t n, float vs
 
 extern "C" size_t tdm_tdf_workspace_bytes(const tdm_grid* g) {
   if (!g) return 0;
-  return (size_t)g->dim[0] * g->dim[1] * g->dim[2];
+  // occupancy bytes + in-plane squared distances (bytes)
+  return 2 * (size_t)g->dim[0] * g->dim[1] * g->dim[2];
 }
 
 extern "C" tdm_status tdm_tdf(const float* pts, int32_t n, const tdm_grid* g, int32_t mode, float* tdf, void* ws,
                               size_t ws_bytes, tdm_stream s) {
   TDM_REQUIRE(pts && g && tdf && ws && n > 0, "tdm_tdf: null pointer or n <= 0");
   TDM_REQUIRE(mode >= 0 && mode <= 2, "tdm_tdf: decode_mode must be 0, 1 or 2");
-  size_t V = tdm_tdf_workspace_bytes(g);
-  TDM_REQUIRE(V > 0 && ws_bytes >= V, "tdm_tdf: workspace too small");
+  const size_t V = (size_t)g->dim[0] * g->dim[1] * g->dim[2];
+  TDM_REQUIRE(V > 0 && ws_bytes >= tdm_tdf_workspace_bytes(g), "tdm_tdf: workspace too small");
   int r = search_radius(g);
   TDM_REQUIRE(r >= 1 && r <= 10, "tdm_tdf: trunc_margin/voxel_size must round to 1..10 voxels");
   uint8_t* occ = static_cast<uint8_t*>(ws);
+  uint8_t* g2 = occ + V;
   TDM_CHECK_CUDA(cudaMemsetAsync(occ, 0, V, s));
   occupancy_kernel<<<(n + 255) / 256, 256, 0, s>>>(pts, n, g->dim[0], g->dim[1], g->dim[2], g->origin[0],
                                                    g->origin[1], g->origin[2], g->voxel_size, occ);
   TDM_CHECK_LAUNCH("occupancy_kernel");
   switch (r) {
-    case 1: launch_tdf_tile<1>(occ, g, tdf, s); break;
-    case 2: launch_tdf_tile<2>(occ, g, tdf, s); break;
-    case 3: launch_tdf_tile<3>(occ, g, tdf, s); break;
-    case 4: launch_tdf_tile<4>(occ, g, tdf, s); break;
-    case 5: launch_tdf_tile<5>(occ, g, tdf, s); break;
-    case 6: launch_tdf_tile<6>(occ, g, tdf, s); break;
-    case 7: launch_tdf_tile<7>(occ, g, tdf, s); break;
-    case 8: launch_tdf_tile<8>(occ, g, tdf, s); break;
-    case 9: launch_tdf_tile<9>(occ, g, tdf, s); break;
-    default: launch_tdf_tile<10>(occ, g, tdf, s); break;
+    case 1: launch_tdf<1>(occ, g2, g, tdf, s); break;
+    case 2: launch_tdf<2>(occ, g2, g, tdf, s); break;
+    case 3: launch_tdf<3>(occ, g2, g, tdf, s); break;
+    case 4: launch_tdf<4>(occ, g2, g, tdf, s); break;
+    case 5: launch_tdf<5>(occ, g2, g, tdf, s); break;
+    case 6: launch_tdf<6>(occ, g2, g, tdf, s); break;
+    case 7: launch_tdf<7>(occ, g2, g, tdf, s); break;
+    case 8: launch_tdf<8>(occ, g2, g, tdf, s); break;
+    case 9: launch_tdf<9>(occ, g2, g, tdf, s); break;
+    default: launch_tdf<10>(occ, g2, g, tdf, s); break;
   }
-  TDM_CHECK_LAUNCH("tdf_tile_kernel");
+  note_launches(1);
+  TDM_CHECK_LAUNCH("tdf_plane_kernel / tdf_z_kernel");
   const int64_t first_bad = (int64_t)1 << 24;
   if (mode != TDM_TDF_EXACT && (int64_t)V > first_bad) {
     int64_t cnt = (int64_t)V - first_bad;

@@ -215,6 +215,70 @@ def run_reference(args, rank, world):
 # --------------------------------------------------------------------------
 # GPU arm
 # --------------------------------------------------------------------------
+def stage_breakdown(tdm, torch, dev, pair, net, k, ransac_iters, prec, reps=5):
+    """Times each stage of one pair with CUDA events (median of reps) and
+    reports its achieved rate against the stage's roofline."""
+    peaks, kind = load_peaks()
+    hbm = peaks["hbm_gbs"]
+    tc_peak = peaks["bf16_tflops"]
+    a, b, _ = pair
+    stream = torch.cuda.current_stream()
+
+    def timeit(fn):
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts)), out
+
+    pd = torch.from_numpy(a).to(dev)
+    g = tdm.grid_from_points_host(a)
+    V = g.voxels
+    ms_tdf, tdf = timeit(lambda: tdm.tdf(pd, g))
+    idx = tdm.keypoint_indices(5, a.shape[0], k, device=dev)
+    kp, kg = tdm.keypoints(pd, idx, g)
+    ms_gather, patches = timeit(lambda: tdm.gather(tdf, g, kg))
+    p2 = torch.cat([patches, patches])
+    ms_net, desc = timeit(lambda: net.forward(p2))
+    mprec = "bf16" if prec in ("bf16", "fp8") else "fp32"
+    ms_mnn, res = timeit(lambda: tdm.match_mnn(desc[:k].contiguous(), desc[k:].contiguous(), mprec))
+    # RANSAC on the real matches of a pair
+    pb = torch.from_numpy(b).to(dev)
+    gb = tdm.grid_from_points_host(b)
+    kpb, kgb = tdm.keypoints(pb, tdm.keypoint_indices(6, b.shape[0], k, device=dev), gb)
+    descb = net.forward(tdm.gather(tdm.tdf(pb, gb), gb, kgb))
+    pairs_, npairs, _, _ = tdm.match_mnn(desc[:k].contiguous(), descb, mprec)
+    x, y = tdm.pairs_to_points(kp, kpb, pairs_, npairs)
+    m = int(npairs.item())
+    ms_ransac, _ = timeit(lambda: tdm.ransac(x, y, npairs, 7, ransac_iters, 0.05))
+
+    def frac(ach, peak):
+        return round(ach / peak, 4)
+
+    tdf_bytes = 12 * a.shape[0] + 4 * V
+    gather_bytes = k * 27000 * 8
+    net_flop = 2 * k * NET_FLOP_PER_PATCH
+    mnn_flop = 2.0 * k * k * 512
+    ransac_flop = ransac_iters * max(m, 1) * 20.0
+    return {
+        "tdf": {"ms": ms_tdf, "bound": "hbm", "achieved_gbs": tdf_bytes / ms_tdf / 1e6,
+                "frac": frac(tdf_bytes / ms_tdf / 1e6, hbm), "work": "12*N + 4*V = %d bytes (V=%d)" % (tdf_bytes, V)},
+        "gather": {"ms": ms_gather, "bound": "hbm", "achieved_gbs": gather_bytes / ms_gather / 1e6,
+                   "frac": frac(gather_bytes / ms_gather / 1e6, hbm), "work": "%d patches x 27000 x 8 B" % k},
+        "net": {"ms": ms_net, "bound": "tensor", "achieved_tflops": net_flop / ms_net / 1e9,
+                "frac": frac(net_flop / ms_net / 1e9, tc_peak), "work": "%d patches x 6.452 GFLOP" % (2 * k)},
+        "mnn": {"ms": ms_mnn, "bound": "tensor", "achieved_tflops": mnn_flop / ms_mnn / 1e9,
+                "frac": frac(mnn_flop / ms_mnn / 1e9, tc_peak), "work": "2 x %d x %d x 512 FLOP" % (k, k)},
+        "ransac": {"ms": ms_ransac, "bound": "fp32 simt", "achieved_tflops": ransac_flop / ms_ransac / 1e9,
+                   "work": "%d trials x %d matches x 20 FLOP" % (ransac_iters, m)},
+        "peak_source": kind + " (hbm_gbs, bf16_tflops burst: stages timed alone)",
+    }
+
+
 def run_ours(args, rank, world, local):
     import torch
     import __graft_entry__ as ge
@@ -339,6 +403,9 @@ def run_ours(args, rank, world, local):
         t0 = time.perf_counter()
         pipe.register(a, b, seed=2000 + s_, k=k)
         lat.append((time.perf_counter() - t0) * 1000.0)
+    # per-stage breakdown of one pair through the stage calls (CUDA events on
+    # the launching stream), each against its roofline
+    stages = stage_breakdown(tdm, torch, dev, pairs[0], net, k, args.ransac_iters, prec)
     # roofline of the dominant kernel: conv2 on tcgen05 (useful FLOPs per launch / event time)
     conv2_ms, conv2_n = lt["conv2"]
     peaks, peak_kind = load_peaks()
@@ -379,6 +446,7 @@ def run_ours(args, rank, world, local):
                        "last_result": {"matches": res.n_matches, "inliers": res.n_inliers} if res else None},
             "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roof,
+            "stages": stages,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches,
