@@ -38,7 +38,8 @@ EXPORTS = [
     "tdm_ransac_workspace_bytes", "tdm_ransac", "tdm_ransac_noalloc", "tdm_pairs_to_points",
     "tdm_tsdf_init", "tdm_depth_from_mm", "tdm_tsdf_integrate", "tdm_extract_workspace_bytes", "tdm_tsdf_extract",
     "tdm_pipeline_create", "tdm_pipeline_destroy", "tdm_describe_fragment", "tdm_register_pair",
-    "tdm_register_pair_host",
+    "tdm_register_pair_host", "tdm_net_clone", "tdm_net_workspace_bytes",
+    "tdm_server_create", "tdm_server_slots", "tdm_server_submit", "tdm_server_wait", "tdm_server_destroy",
 ]
 
 
@@ -69,6 +70,10 @@ class PipelineConfig(ctypes.Structure):
     _fields_ = [("voxel_size", ctypes.c_float), ("trunc_voxels", ctypes.c_float), ("pad", ctypes.c_int32),
                 ("max_points", ctypes.c_int32), ("max_keypoints", ctypes.c_int32), ("max_voxels", ctypes.c_int64),
                 ("match_precision", ctypes.c_int32), ("ransac", RansacParams)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("pipeline", PipelineConfig), ("slots", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64)]
 
 
 class PairResult(ctypes.Structure):
@@ -131,6 +136,13 @@ def lib():
         "tdm_describe_fragment": (i32, [P, P, i32, u64, i32, P, P, G, P]),
         "tdm_register_pair": (i32, [P, P, i32, P, i32, u64, i32, ctypes.POINTER(PairResult), P]),
         "tdm_register_pair_host": (i32, [P, P, i32, P, i32, u64, i32, ctypes.POINTER(PairResult), P]),
+        "tdm_net_clone": (i32, [P, ctypes.POINTER(P)]),
+        "tdm_net_workspace_bytes": (sz, [P, i32]),
+        "tdm_server_create": (i32, [ctypes.POINTER(ServerConfig), P, ctypes.POINTER(P)]),
+        "tdm_server_slots": (i32, [P]),
+        "tdm_server_submit": (i32, [P, P, i32, P, i32, u64, i32, ctypes.POINTER(ctypes.c_int64)]),
+        "tdm_server_wait": (i32, [P, ctypes.c_int64, ctypes.POINTER(PairResult), ctypes.POINTER(ctypes.c_double)]),
+        "tdm_server_destroy": (i32, [P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name, None)
@@ -399,13 +411,17 @@ def tsdf_extract(tsdf_dev, weight_dev, dim, origin, voxel_size, tsdf_thr=0.2, w_
 # --------------------------------------------------------------------------
 # Whole path
 # --------------------------------------------------------------------------
+def pipeline_config(voxel_size=0.01, trunc_voxels=5.0, pad=15, max_points=400000, max_keypoints=5000,
+                    max_voxels=120_000_000, match_precision="fp32", ransac_seed=7, ransac_iters=100000, threshold=0.05,
+                    adaptive=False, max_trials=50000) -> PipelineConfig:
+    return PipelineConfig(voxel_size, trunc_voxels, pad, max_points, max_keypoints, max_voxels,
+                          PRECISIONS[match_precision],
+                          RansacParams(ransac_seed, ransac_iters, threshold, 1 if adaptive else 0, max_trials))
+
+
 class Pipeline:
-    def __init__(self, net: Net, voxel_size=0.01, trunc_voxels=5.0, pad=15, max_points=400000, max_keypoints=5000,
-                 max_voxels=120_000_000, match_precision="fp32", ransac_seed=7, ransac_iters=100000,
-                 threshold=0.05, adaptive=False, max_trials=50000):
-        cfg = PipelineConfig(voxel_size, trunc_voxels, pad, max_points, max_keypoints, max_voxels,
-                             PRECISIONS[match_precision],
-                             RansacParams(ransac_seed, ransac_iters, threshold, 1 if adaptive else 0, max_trials))
+    def __init__(self, net: Net, **kw):
+        cfg = pipeline_config(**kw)
         h = ctypes.c_void_p()
         check(lib().tdm_pipeline_create(ctypes.byref(cfg), net.handle, ctypes.byref(h)))
         self.handle = h
@@ -435,6 +451,45 @@ class Pipeline:
     def close(self):
         if self.handle:
             lib().tdm_pipeline_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop: requests queue up and run on min(slots, budget / slot
+    footprint) concurrent slots (own stream, buffers and net clone each)."""
+
+    def __init__(self, net: Net, slots=4, hbm_budget_bytes=120 << 30, **pipeline_kw):
+        cfg = ServerConfig(pipeline_config(**pipeline_kw), slots, hbm_budget_bytes)
+        h = ctypes.c_void_p()
+        check(lib().tdm_server_create(ctypes.byref(cfg), net.handle, ctypes.byref(h)))
+        self.handle = h
+
+    @property
+    def slots(self) -> int:
+        return int(lib().tdm_server_slots(self.handle))
+
+    def submit(self, pts_a: np.ndarray, pts_b: np.ndarray, seed: int, k: int) -> int:
+        a = np.ascontiguousarray(pts_a, np.float32)
+        b = np.ascontiguousarray(pts_b, np.float32)
+        t = ctypes.c_int64()
+        check(lib().tdm_server_submit(self.handle, _ptr(a), a.shape[0], _ptr(b), b.shape[0], seed, k, ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int):
+        r = PairResult()
+        lat = ctypes.c_double()
+        check(lib().tdm_server_wait(self.handle, ticket, ctypes.byref(r), ctypes.byref(lat)))
+        return r, lat.value
+
+    def close(self):
+        if self.handle:
+            lib().tdm_server_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

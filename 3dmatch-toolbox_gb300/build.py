@@ -107,7 +107,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         objs = list(ex.map(lambda s: _compile(s, hdrs), srcs))
     if _stale(LIB_PATH, objs):
         tmp = LIB_PATH + ".tmp%d" % os.getpid()
-        _run([_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        _run([_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
         os.replace(tmp, LIB_PATH)
     for tool in ("demo", "fuse"):
         src = os.path.join(HOST, tool + ".cpp")

@@ -33,6 +33,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <cstring>
 #include <vector>
 
@@ -420,8 +421,14 @@ tdm_status launch_t(const KParams& kp, size_t smem, cudaStream_t s) {
   // Every tcgen05 CTA takes more than half an SM's shared memory, so two
   // TMEM-allocating CTAs never share an SM.
   size_t req = std::max<size_t>(smem, 120 * 1024);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)req);
-  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(tc_conv_kernel)");
+  // The attribute is a cap shared by every launch of this instantiation (from
+  // any host thread): raise it once to the full budget.
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [&] {
+    attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  });
+  if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_kernel)");
   int64_t grid = std::min<int64_t>(kp.total_tiles, sm_count());
   kern<<<(unsigned)std::max<int64_t>(grid, 1), kThreads, req, s>>>(kp);
   TDM_CHECK_LAUNCH("tc_conv_kernel");

@@ -681,3 +681,27 @@ extern "C" tdm_status tdm_write_seeded_weights(const char* path, uint64_t seed) 
   if (st != TDM_OK) return fail(st, err);
   return TDM_OK;
 }
+
+extern "C" tdm_status tdm_net_clone(const tdm_net* src, tdm_net** out) {
+  TDM_REQUIRE(src && out, "tdm_net_clone: null pointer");
+  const float* w[9];
+  const float* b[9];
+  for (int l = 0; l < 9; ++l) {
+    w[l] = src->hw[l].data();
+    b[l] = src->hb[l].data();
+  }
+  tdm_net* net = nullptr;
+  tdm_status st = tdm_net_create_from_host(w, b, src->prec, src->use_feat, &net);
+  if (st) return st;
+  for (int l = 0; l < 9; ++l) net->act_scale[l] = src->act_scale[l];
+  net->calibrated = src->calibrated;
+  net->max_batch = src->max_batch;
+  *out = net;
+  return TDM_OK;
+}
+
+extern "C" size_t tdm_net_workspace_bytes(const tdm_net* net, int32_t b) {
+  if (!net || b <= 0) return 0;
+  const int chunk = std::min<int>(b, net->max_batch);
+  return net->prec == TDM_FP32 ? f32_ws_bytes(chunk) : bf16_plan(net, chunk).total;
+}

@@ -305,6 +305,16 @@ __global__ void pairs_to_points_kernel(const float* __restrict__ ka, const float
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Raises trials_kernel's dynamic shared-memory cap once (any host thread).
+cudaError_t trials_smem_cap() {
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [] {
+    err = cudaFuncSetAttribute(trials_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * 4096 * 4);
+  });
+  return err;
+}
+
 }  // namespace
 }  // namespace tdm
 
@@ -330,9 +340,7 @@ extern "C" tdm_status tdm_ransac(const float* x, const float* y, const int32_t* 
   if (iters > 0) {
     int smem_pts = m_max <= 4096 ? m_max : 0;  // 96 KB of correspondences at most
     size_t smem = (size_t)6 * smem_pts * sizeof(float);
-    if (smem > 48 * 1024) {
-      TDM_CHECK_CUDA(cudaFuncSetAttribute(trials_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    }
+    TDM_CHECK_CUDA(trials_smem_cap());
     trials_kernel<<<(iters + 255) / 256, 256, smem, s>>>(x, y, m_dev, m_max, smem_pts, prm->seed, iters,
                                                           prm->threshold, counts, best);
     TDM_CHECK_LAUNCH("trials_kernel");
@@ -423,9 +431,7 @@ extern "C" tdm_status tdm_ransac_noalloc(const float* x, const float* y, const i
   if (iters > 0) {
     int smem_pts = m_max <= 4096 ? m_max : 0;
     size_t smem = (size_t)6 * smem_pts * sizeof(float);
-    if (smem > 48 * 1024) {
-      TDM_CHECK_CUDA(cudaFuncSetAttribute(trials_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    }
+    TDM_CHECK_CUDA(trials_smem_cap());
     trials_kernel<<<(iters + 255) / 256, 256, smem, s>>>(x, y, m_dev, m_max, smem_pts, prm->seed, iters,
                                                           prm->threshold, counts, best);
     TDM_CHECK_LAUNCH("trials_kernel (noalloc)");

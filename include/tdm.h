@@ -119,6 +119,11 @@ tdm_status tdm_net_response(tdm_net* net, const char* name, const float* patches
  * FP8 forward.  tdm_net_act_scales returns the 9 scales (index = layer). */
 tdm_status tdm_net_calibrate(tdm_net* net, const float* patches_dev, int32_t b, tdm_stream s);
 tdm_status tdm_net_act_scales(tdm_net* net, float* scales);
+/* A second net with the same weights, precision and FP8 scales (one per
+ * concurrent stream: a net's activation workspace serves one call at a time). */
+tdm_status tdm_net_clone(const tdm_net* src, tdm_net** out);
+/* Device bytes of the activation workspace a forward of b patches allocates. */
+size_t tdm_net_workspace_bytes(const tdm_net* net, int32_t b);
 /* Patches per internal chunk (bounds the activation workspace; default 2048). */
 tdm_status tdm_net_set_max_batch(tdm_net* net, int32_t max_batch);
 /* Per-layer device time, the analogue of Marvin's debug_mode tic/toc
@@ -231,6 +236,28 @@ tdm_status tdm_register_pair(tdm_pipeline* p, const float* pts_a_dev, int32_t na
 /* Whole pair from host points (host->device copies inside the call). */
 tdm_status tdm_register_pair_host(tdm_pipeline* p, const float* pts_a_host, int32_t na, const float* pts_b_host,
                                   int32_t nb, uint64_t seed, int32_t k, tdm_pair_result* result, tdm_stream s);
+
+/* ---- serving: pair-registration requests of different sizes as they arrive
+ * (the reference registers pairs one by one through files and MATLAB,
+ * evaluation/geometric-registration/register2Fragments.m) --------------------- */
+typedef struct tdm_server tdm_server;
+typedef struct tdm_server_config {
+  tdm_pipeline_config pipeline; /* per-slot limits = the largest admitted request */
+  int32_t slots;                /* concurrent slots requested */
+  int64_t hbm_budget_bytes;     /* slots are created only while their device footprint fits */
+} tdm_server_config;
+/* Creates min(slots, budget / slot footprint) slots, each with its own stream,
+ * pipeline and clone of `net`, and one worker thread per slot. */
+tdm_status tdm_server_create(const tdm_server_config* cfg, const tdm_net* net, tdm_server** out);
+int32_t tdm_server_slots(const tdm_server* s);
+/* Queues a request (points copied; the caller's buffers may be reused at once).
+ * Requests beyond the slot limits are refused (TDM_ERR_INVALID_ARG). */
+tdm_status tdm_server_submit(tdm_server* s, const float* pts_a_host, int32_t na, const float* pts_b_host, int32_t nb,
+                             uint64_t seed, int32_t k, int64_t* ticket);
+/* Blocks until the ticket's result is ready; latency is submit-to-completion. */
+tdm_status tdm_server_wait(tdm_server* s, int64_t ticket, tdm_pair_result* result, double* latency_ms);
+/* Finishes queued requests, then stops the workers and frees the slots. */
+tdm_status tdm_server_destroy(tdm_server* s);
 
 #ifdef __cplusplus
 }
