@@ -38,7 +38,9 @@ int* device_error_word() {
   if (!words[dev]) {
     int* p = nullptr;
     if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) return nullptr;
-    if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess) return nullptr;
+    // cudaMemset is queued on the legacy stream, which kernels on
+    // non-blocking streams do not wait for: finish it before publishing
+    if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return nullptr;
     words[dev] = p;
   }
   return words[dev];

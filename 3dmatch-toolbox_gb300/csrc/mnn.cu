@@ -22,10 +22,32 @@ constexpr int TOPK = 4;
 
 __device__ __forceinline__ bool better(float d, int j, float bd, int bj) { return d < bd || (d == bd && j < bj); }
 
+// float -> double by moving the fields (exact, integer pipe); zeros,
+// subnormals, infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ double f2d(float x) {
+  const uint32_t u = __float_as_uint(x), e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)x;
+  const uint64_t bits = ((uint64_t)(u >> 31) << 63) | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// sum_k (a_k - b_k)^2 in double, k in order, one fma per term (the oracle's
+// expression).  GB300 issues an FP64 warp instruction at a small fraction of
+// the FP32 rate whatever the number of active lanes, so callers keep all 32
+// lanes busy with independent (query, candidate) pairs.
 __device__ __forceinline__ double exact_sqdist(const float* __restrict__ a, const float* __restrict__ b, int dim) {
   double s = 0.0;
-  for (int k = 0; k < dim; ++k) {
-    double d = (double)a[k] - (double)b[k];
+#pragma unroll 4
+  for (int k = 0; k < dim; k += 4) {
+    const float4 x = *reinterpret_cast<const float4*>(a + k);
+    const float4 y = *reinterpret_cast<const float4*>(b + k);
+    double d = f2d(x.x) - f2d(y.x);
+    s = fma(d, d, s);
+    d = f2d(x.y) - f2d(y.y);
+    s = fma(d, d, s);
+    d = f2d(x.z) - f2d(y.z);
+    s = fma(d, d, s);
+    d = f2d(x.w) - f2d(y.w);
     s = fma(d, d, s);
   }
   return s;
@@ -122,48 +144,167 @@ __device__ __forceinline__ Cand warp_merge(const Cand& mine) {
   return out;
 }
 
-// Row pass: warp per query row i of `dot` [nq][ld]; distances d = nq_i + nr_j - 2 dot.
-// Candidates re-scored in FP64; `fallback` rows scanned completely in FP64.
+// Candidate lists: cand[g][0..3] for query g (rows of a first, then the
+// columns, i.e. the rows of b).  cand[g][0] == -1 marks a query whose list is
+// closer than twice the FP32 error bound of the expansion (FP32 form only);
+// such a query is appended to `full` and scanned completely in FP64.
+__device__ __forceinline__ void put_candidates(const Cand& m, float qn, float rn_max, int nr, int dim, int exact,
+                                               int g, int32_t* __restrict__ cand, int32_t* __restrict__ full,
+                                               int32_t* __restrict__ n_full) {
+  const float sq = sqrtf(qn) + sqrtf(rn_max);
+  const float E = 2.0f * (float)(dim + 8) * 5.97e-8f * sq * sq;
+  if (exact && nr > TOPK && m.d[TOPK - 1] - m.d[0] < 2.0f * E) {
+    cand[4 * g] = -1;
+    full[atomicAdd(n_full, 1)] = g;
+    return;
+  }
+#pragma unroll
+  for (int t = 0; t < TOPK; ++t) cand[4 * g + t] = m.j[t];
+}
+
+// Row scan: warp per query row i of `dot` [nq][ld]; d = qn_i + rn_j - 2 dot.
 __global__ void nn_rows_kernel(const float* __restrict__ dot, int64_t ld, int nq, int nr,
                                const float* __restrict__ qn, const float* __restrict__ rn,
-                               const float* __restrict__ rn_max_ptr,
-                               const float* __restrict__ q, const float* __restrict__ r, int dim, int transposed,
-                               int exact, int32_t* __restrict__ nn) {
+                               const float* __restrict__ rn_max_ptr, int dim, int exact, int32_t* __restrict__ cand,
+                               int32_t* __restrict__ full, int32_t* __restrict__ n_full) {
   const int warps = blockDim.x / 32, lane = threadIdx.x & 31;
   const int i = blockIdx.x * warps + threadIdx.x / 32;
   if (i >= nq) return;
   Cand c;
   cand_init(c);
-  for (int j = lane; j < nr; j += 32) {
-    float dp = transposed ? dot[(int64_t)j * ld + i] : dot[(int64_t)i * ld + j];
-    float d = qn[i] + rn[j] - 2.0f * dp;
-    cand_push(c, d, j);
+  const float qi = qn[i];
+  // four columns per lane per step: one 512-byte coalesced read per warp
+  const float* row = dot + (int64_t)i * ld;
+  for (int j = 4 * lane; j < nr; j += 128) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(row + j));
+    const float4 n = __ldg(reinterpret_cast<const float4*>(rn + j));
+    cand_push(c, qi + n.x - 2.0f * v.x, j);
+    if (j + 1 < nr) cand_push(c, qi + n.y - 2.0f * v.y, j + 1);
+    if (j + 2 < nr) cand_push(c, qi + n.z - 2.0f * v.z, j + 2);
+    if (j + 3 < nr) cand_push(c, qi + n.w - 2.0f * v.w, j + 3);
   }
   Cand m = warp_merge(c);
-  // error bound of the FP32 expansion (dot of length dim, sequential fma)
-  const float sq = sqrtf(qn[i]) + sqrtf(*rn_max_ptr);
-  const float E = 2.0f * (float)(dim + 8) * 5.97e-8f * sq * sq;
-  const bool full = exact && (m.d[TOPK - 1] - m.d[0] < 2.0f * E) && nr > TOPK;
-  const float* qi = q + (int64_t)i * dim;
+  if (lane == 0) put_candidates(m, qi, *rn_max_ptr, nr, dim, exact, i, cand, full, n_full);
+}
+
+// Column scan over `dot` [nr][ld]: query j is a column, candidates are the
+// rows i.  A block owns 32 consecutive columns (lane = column) and its 16
+// warps split the rows, so each row read is one coalesced 128-byte line; the
+// per-warp lists are merged in shared memory.  Query index g = goff + j.
+constexpr int COL_WARPS = 16;
+
+__global__ void __launch_bounds__(COL_WARPS * 32)
+nn_cols_kernel(const float* __restrict__ dot, int64_t ld, int nq, int nr, const float* __restrict__ qn,
+               const float* __restrict__ rn, const float* __restrict__ rn_max_ptr, int dim, int exact, int goff,
+               int32_t* __restrict__ cand, int32_t* __restrict__ full, int32_t* __restrict__ n_full) {
+  __shared__ float s_d[COL_WARPS][TOPK][32];
+  __shared__ int s_j[COL_WARPS][TOPK][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
+  const bool live = j < nq;
+  Cand c;
+  cand_init(c);
+  if (live) {
+    const float qj = qn[j];
+    int i = w;
+    for (; i + 3 * COL_WARPS < nr; i += 4 * COL_WARPS) {  // four rows in flight
+      float v[4], n[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        v[u] = __ldg(dot + (int64_t)(i + u * COL_WARPS) * ld + j);
+        n[u] = __ldg(rn + i + u * COL_WARPS);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) cand_push(c, qj + n[u] - 2.0f * v[u], i + u * COL_WARPS);
+    }
+    for (; i < nr; i += COL_WARPS) cand_push(c, qj + __ldg(rn + i) - 2.0f * __ldg(dot + (int64_t)i * ld + j), i);
+  }
+#pragma unroll
+  for (int t = 0; t < TOPK; ++t) { s_d[w][t][lane] = c.d[t]; s_j[w][t][lane] = c.j[t]; }
+  __syncthreads();
+  if (w == 0 && live) {
+    Cand m;
+    cand_init(m);
+    for (int v = 0; v < COL_WARPS; ++v)
+#pragma unroll
+      for (int t = 0; t < TOPK; ++t) cand_push(m, s_d[v][t][lane], s_j[v][t][lane]);
+    put_candidates(m, qn[j], *rn_max_ptr, nr, dim, exact, goff + j, cand, full, n_full);
+  }
+}
+
+// Query g < na: a_g against the rows of b (result nn_ab[g]); otherwise
+// b_{g-na} against the rows of a (nn_ba[g-na]).
+struct Query {
+  const float* q;
+  const float* r;
+  int nr;
+  int32_t* out;
+};
+
+__device__ __forceinline__ Query query_of(int g, const float* a, const float* b, int na, int nb, int dim,
+                                          int32_t* nn_ab, int32_t* nn_ba) {
+  if (g < na) return Query{a + (int64_t)g * dim, b, nb, nn_ab + g};
+  return Query{b + (int64_t)(g - na) * dim, a, na, nn_ba + (g - na)};
+}
+
+// Re-scoring: four consecutive lanes hold the four candidates of one query;
+// the exact minimum (ties -> lower index) is reduced over those lanes.
+__global__ void rescore_kernel(const float* __restrict__ a, const float* __restrict__ b, int na, int nb, int dim,
+                               const int32_t* __restrict__ cand, int32_t* __restrict__ nn_ab,
+                               int32_t* __restrict__ nn_ba) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = (int)(t >> 2);
   double best = DBL_MAX;
   int bj = INT_MAX;
-  if (!full) {
-    if (lane < TOPK && m.j[lane] < nr) {
-      best = exact_sqdist(qi, r + (int64_t)m.j[lane] * dim, dim);
-      bj = m.j[lane];
-    }
-  } else {
-    for (int j = lane; j < nr; j += 32) {
-      double d = exact_sqdist(qi, r + (int64_t)j * dim, dim);
-      if (d < best || (d == best && j < bj)) { best = d; bj = j; }
+  bool skip = true;
+  Query Q{};
+  if (g < na + nb) {
+    Q = query_of(g, a, b, na, nb, dim, nn_ab, nn_ba);
+    skip = cand[4 * g] == -1;
+    const int j = cand[t];
+    if (!skip && j >= 0 && j < Q.nr) {
+      best = exact_sqdist(Q.q, Q.r + (int64_t)j * dim, dim);
+      bj = j;
     }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    double od = __shfl_xor_sync(0xffffffffu, best, o);
-    int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+  for (int o = 1; o < 4; o <<= 1) {
+    const double od = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
     if (od < best || (od == best && oj < bj)) { best = od; bj = oj; }
   }
-  if (lane == 0) nn[i] = bj;
+  if (!skip && (t & 3) == 0) *Q.out = bj;
+}
+
+// Full FP64 scan of the listed queries, one block per query at a time.
+__global__ void full_scan_kernel(const float* __restrict__ a, const float* __restrict__ b, int na, int nb, int dim,
+                                 const int32_t* __restrict__ full, const int32_t* __restrict__ n_full,
+                                 int32_t* __restrict__ nn_ab, int32_t* __restrict__ nn_ba) {
+  __shared__ double s_d[32];
+  __shared__ int s_i[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int n = *n_full;
+  for (int e = blockIdx.x; e < n; e += gridDim.x) {
+    const Query Q = query_of(full[e], a, b, na, nb, dim, nn_ab, nn_ba);
+    double best = DBL_MAX;
+    int bi = INT_MAX;
+    for (int i = threadIdx.x; i < Q.nr; i += blockDim.x) {
+      const double d = exact_sqdist(Q.q, Q.r + (int64_t)i * dim, dim);
+      if (d < best) { best = d; bi = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double od = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (od < best || (od == best && oi < bi)) { best = od; bi = oi; }
+    }
+    if (lane == 0) { s_d[w] = best; s_i[w] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int v = 1; v < nw; ++v)
+        if (s_d[v] < best || (s_d[v] == best && s_i[v] < bi)) { best = s_d[v]; bi = s_i[v]; }
+      *Q.out = bi;
+    }
+    __syncthreads();
+  }
 }
 
 // Mutual check and ordered compaction (one block): pairs (nn_ba[j], j).
@@ -218,7 +359,7 @@ __global__ void max_kernel(const float* __restrict__ x, int n, float* __restrict
 
 struct MnnLayout {
   int nbp;
-  size_t dot, bT, na_n, nb_n, maxes, a8, bpk, zeros, total;
+  size_t dot, bT, na_n, nb_n, maxes, a8, bpk, zeros, cand, full, total;
   int64_t a8_cs;
 };
 
@@ -235,7 +376,9 @@ MnnLayout mnn_layout(int na, int nb, int dim) {
   L.a8_cs = ((int64_t)na + 256 + 16) * 16;
   L.a8 = take((size_t)(dim / 8) * L.a8_cs);
   L.bpk = take((size_t)L.nbp * (dim / 8) * 16);
-  L.zeros = take((size_t)L.nbp * 4);
+  L.zeros = take((size_t)L.nbp * 4 + 16);  // zero bias row, then the full-scan counter
+  L.cand = take((size_t)(na + nb) * TOPK * 4);
+  L.full = take((size_t)(na + nb) * 4);
   L.total = off;
   return L;
 }
@@ -256,6 +399,7 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
   TDM_REQUIRE(da && db && nn_ab && nn_ba && pairs && n_pairs && ws, "tdm_match_mnn: null pointer");
   TDM_REQUIRE(na > 0 && nb > 0, "tdm_match_mnn: empty descriptor set");
   TDM_REQUIRE(dim % 64 == 0, "tdm_match_mnn: dim must be a multiple of 64");
+  TDM_REQUIRE(((uintptr_t)da | (uintptr_t)db) % 16 == 0, "tdm_match_mnn: descriptors must be 16-byte aligned");
   TDM_REQUIRE(prec == TDM_FP32 || prec == TDM_BF16, "tdm_match_mnn: precision must be FP32 or BF16");
   MnnLayout L = mnn_layout(na, nb, dim);
   TDM_REQUIRE(ws_bytes >= L.total, "tdm_match_mnn: workspace too small");
@@ -271,7 +415,10 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
   note_launches(3);
   TDM_CHECK_LAUNCH("mnn norms");
   float* zeros = reinterpret_cast<float*>(w + L.zeros);
-  TDM_CHECK_CUDA(cudaMemsetAsync(zeros, 0, (size_t)L.nbp * 4, s));
+  int32_t* n_full = reinterpret_cast<int32_t*>(zeros + L.nbp);
+  int32_t* cand = reinterpret_cast<int32_t*>(w + L.cand);
+  int32_t* full = reinterpret_cast<int32_t*>(w + L.full);
+  TDM_CHECK_CUDA(cudaMemsetAsync(zeros, 0, (size_t)L.nbp * 4 + 16, s));
   if (prec == TDM_FP32) {
     float* bT = reinterpret_cast<float*>(w + L.bT);
     int64_t n = (int64_t)dim * L.nbp;
@@ -311,11 +458,18 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
     if (st) return st;
   }
   const int exact = prec == TDM_FP32 ? 1 : 0;
-  // rows: a -> b ; columns: b -> a (dot read transposed)
-  nn_rows_kernel<<<(na + 7) / 8, 256, 0, s>>>(dot, L.nbp, na, nb, an, bn, maxes + 1, da, db, dim, 0, exact, nn_ab);
-  nn_rows_kernel<<<(nb + 7) / 8, 256, 0, s>>>(dot, L.nbp, nb, na, bn, an, maxes, db, da, dim, 1, exact, nn_ba);
-  note_launches(1);
-  TDM_CHECK_LAUNCH("nn_rows_kernel");
+  // candidates: rows a -> b (warp per row), columns b -> a (32 columns per block)
+  nn_rows_kernel<<<(na + 7) / 8, 256, 0, s>>>(dot, L.nbp, na, nb, an, bn, maxes + 1, dim, exact, cand, full, n_full);
+  nn_cols_kernel<<<(nb + 31) / 32, COL_WARPS * 32, 0, s>>>(dot, L.nbp, nb, na, bn, an, maxes, dim, exact, na, cand,
+                                                          full, n_full);
+  const int64_t lanes = (int64_t)(na + nb) * TOPK;
+  rescore_kernel<<<(unsigned)((lanes + 127) / 128), 128, 0, s>>>(da, db, na, nb, dim, cand, nn_ab, nn_ba);
+  note_launches(2);
+  if (exact) {
+    full_scan_kernel<<<256, 256, 0, s>>>(da, db, na, nb, dim, full, n_full, nn_ab, nn_ba);
+    note_launches(1);
+  }
+  TDM_CHECK_LAUNCH("mnn candidate scans / re-scoring");
   mutual_kernel<<<1, 992, 0, s>>>(nn_ab, nn_ba, na, nb, pairs, n_pairs);
   TDM_CHECK_LAUNCH("mutual_kernel");
   return TDM_OK;

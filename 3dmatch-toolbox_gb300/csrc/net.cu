@@ -481,7 +481,10 @@ tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, in
   return TDM_OK;
 }
 
-tdm_status ensure_ws(tdm_net* net, size_t bytes) {
+// The zero fill runs on the caller's stream: a plain cudaMemset would be
+// queued on the legacy stream, which a non-blocking caller stream does not
+// wait for, and could land after the forward's first writes.
+tdm_status ensure_ws(tdm_net* net, size_t bytes, cudaStream_t s) {
   if (net->ws_bytes >= bytes) return TDM_OK;
   if (net->ws) {
     TDM_CHECK_CUDA(cudaDeviceSynchronize());
@@ -492,8 +495,9 @@ tdm_status ensure_ws(tdm_net* net, size_t bytes) {
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, bytes);
   if (e != cudaSuccess) return cuda_status(e, "net workspace");
-  TDM_CHECK_CUDA(cudaMemset(p, 0, bytes));
   net->ws = static_cast<uint8_t*>(p);
+  net->ws_bytes = 0;
+  TDM_CHECK_CUDA(cudaMemsetAsync(p, 0, bytes, s));
   net->ws_bytes = bytes;
   return TDM_OK;
 }
@@ -517,6 +521,9 @@ extern "C" tdm_status tdm_net_create_from_host(const float* const* w, const floa
   tdm_net* net = new tdm_net();
   tdm_status st = load_host_weights(net, w, b);
   if (st == TDM_OK) st = create_common(net, prec, use_feat);
+  // cudaMemcpy from pageable memory may return before its DMA lands; the
+  // handle is used next on streams that do not wait for the legacy stream
+  if (st == TDM_OK && cudaDeviceSynchronize() != cudaSuccess) st = fail(TDM_ERR_DEVICE, "weight upload failed");
   if (st != TDM_OK) {
     delete net;
     return st;
@@ -556,7 +563,7 @@ static tdm_status net_run(tdm_net* net, const float* patches, int32_t b, float* 
               "FP8 net has no activation scales yet: call tdm_net_calibrate first");
   const int chunk = std::min<int>(b, net->max_batch);
   size_t need = net->prec == TDM_FP32 ? f32_ws_bytes(chunk) : bf16_plan(net, chunk).total;
-  tdm_status st = ensure_ws(net, need);
+  tdm_status st = ensure_ws(net, need, s);
   if (st) return st;
   size_t per = 512;
   if (stop >= 0) {

@@ -142,7 +142,9 @@ tdm_status tdm_write_seeded_weights(const char* marvin_path, uint64_t seed);
 /* nn_ab[i] = argmin_j |a_i - b_j|, nn_ba likewise; pairs (nn_ba[j], j) for every
  * j with nn_ab[nn_ba[j]] == j, in increasing j.  FP32: exact FP64 refinement of
  * the FP32 candidates (indices equal the exact double-precision NN); BF16:
- * tcgen05 distance GEMM.  pairs_dev: 2*min(na,nb) int32; n_pairs_dev: 1 int32. */
+ * tcgen05 distance GEMM, its 4 best candidates per query re-scored in FP64.
+ * da_dev/db_dev 16-byte aligned, dim a multiple of 64.
+ * pairs_dev: 2*min(na,nb) int32; n_pairs_dev: 1 int32. */
 size_t tdm_mnn_workspace_bytes(int32_t na, int32_t nb, int32_t dim);
 tdm_status tdm_match_mnn(const float* da_dev, int32_t na, const float* db_dev, int32_t nb, int32_t dim,
                          tdm_precision precision, int32_t* nn_ab_dev, int32_t* nn_ba_dev, int32_t* pairs_dev,

@@ -56,6 +56,24 @@ def test_mnn_fp32_ties_and_near_ties(tdm, oracle, cuda):
     assert np.array_equal(pairs, ref_pairs)
 
 
+def test_mnn_fp32_zeros_subnormals_scales(tdm, oracle, cuda):
+    """Zero and subnormal components and rows spanning many magnitudes keep
+    the exact FP64 scores (the float -> double widening of every component)."""
+    rng = np.random.default_rng(11)
+    a = rng.normal(size=(200, 512)).astype(np.float32)
+    b = a[rng.permutation(200)] + 0.2 * rng.normal(size=(200, 512)).astype(np.float32)
+    a[::3, ::5] = 0.0
+    b[1::4, 3::7] = 0.0
+    a[::7, :16] = np.float32(1e-39)  # subnormal
+    b[::5, 100:110] = np.float32(-3e-40)
+    a[::11] *= np.float32(1e-12)
+    b[::13] *= np.float32(1e3)
+    pairs, nn_ab, nn_ba = _run(tdm, cuda, a, b, "fp32")
+    ref_pairs, ref_ab, ref_ba = oracle.mutual_nn(a, b)
+    assert np.array_equal(nn_ab, ref_ab) and np.array_equal(nn_ba, ref_ba)
+    assert np.array_equal(pairs, ref_pairs)
+
+
 @pytest.mark.parametrize("n", [1000, 5000])
 def test_mnn_bf16_agreement(tdm, oracle, cuda, n):
     rng = np.random.default_rng(n)

@@ -160,3 +160,30 @@ def test_fp8_descriptors(tdm, oracle, fp8_net, weights, patches):
     print("fp8 descriptor rel-L2 vs FP64:", err)
     assert err <= 0.1
     tdm.device_status()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_fresh_nets_on_nonblocking_streams(tdm, weights, patches, precision):
+    """The first forward of new nets, issued at once from several threads on
+    streams that do not wait for the legacy stream, equals a settled forward
+    (workspace zeroing and weight uploads are ordered before first use)."""
+    import threading
+    import torch
+    ref = tdm.Net(weights, precision=precision).forward(patches)
+    torch.cuda.synchronize()
+    nets = [tdm.Net(weights, precision=precision) for _ in range(4)]
+    outs = [None] * 4
+
+    def run(t):
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            outs[t] = nets[t].forward(patches, stream=s)
+            s.synchronize()
+
+    th = [threading.Thread(target=run, args=(t,)) for t in range(4)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    for t in range(4):
+        assert torch.equal(outs[t], ref), t
