@@ -40,6 +40,8 @@ EXPORTS = [
     "tdm_pipeline_create", "tdm_pipeline_destroy", "tdm_describe_fragment", "tdm_register_pair",
     "tdm_register_pair_host", "tdm_net_clone", "tdm_net_workspace_bytes",
     "tdm_server_create", "tdm_server_slots", "tdm_server_submit", "tdm_server_wait", "tdm_server_destroy",
+    "tdm_net_autotune", "tdm_net_tiles", "tdm_net_set_tile",
+    "tdm_batch_create", "tdm_batch_destroy", "tdm_batch_device_bytes", "tdm_describe_batch", "tdm_batch_stats",
 ]
 
 
@@ -70,6 +72,12 @@ class PipelineConfig(ctypes.Structure):
     _fields_ = [("voxel_size", ctypes.c_float), ("trunc_voxels", ctypes.c_float), ("pad", ctypes.c_int32),
                 ("max_points", ctypes.c_int32), ("max_keypoints", ctypes.c_int32), ("max_voxels", ctypes.c_int64),
                 ("match_precision", ctypes.c_int32), ("ransac", RansacParams)]
+
+
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("max_fragments", ctypes.c_int32), ("max_points", ctypes.c_int64), ("max_keypoints", ctypes.c_int64),
+                ("max_voxels", ctypes.c_int64), ("trunc_voxels", ctypes.c_float), ("pad", ctypes.c_int32),
+                ("use_graph", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -143,6 +151,14 @@ def lib():
         "tdm_server_submit": (i32, [P, P, i32, P, i32, u64, i32, ctypes.POINTER(ctypes.c_int64)]),
         "tdm_server_wait": (i32, [P, ctypes.c_int64, ctypes.POINTER(PairResult), ctypes.POINTER(ctypes.c_double)]),
         "tdm_server_destroy": (i32, [P]),
+        "tdm_net_autotune": (i32, [P, P, i32, i32, P]),
+        "tdm_net_tiles": (i32, [P, P, P]),
+        "tdm_net_set_tile": (i32, [P, i32, i32, i32]),
+        "tdm_batch_create": (i32, [ctypes.POINTER(BatchConfig), P, ctypes.POINTER(P)]),
+        "tdm_batch_destroy": (i32, [P]),
+        "tdm_batch_device_bytes": (sz, [P]),
+        "tdm_describe_batch": (i32, [P, P, i32, P, P, P, P, P, P, P, P]),
+        "tdm_batch_stats": (i32, [P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name, None)
@@ -309,6 +325,21 @@ class Net:
         check(lib().tdm_net_layer_times(self.handle, _ptr(ms), _ptr(n), 1 if reset else 0))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.LAYER_SLOTS)}
 
+    def autotune(self, patches_dev, reps: int = 3, stream=None) -> dict:
+        """Per-layer tcgen05 tile chosen by timing every shape on these patches."""
+        check(lib().tdm_net_autotune(self.handle, _ptr(patches_dev), patches_dev.shape[0], reps, _stream(stream)))
+        return self.tiles()
+
+    def tiles(self) -> dict:
+        """{layer: (N tile, M sub-tiles)} of the tensor-core forms."""
+        nt = np.zeros(9, np.int32)
+        ms = np.zeros(9, np.int32)
+        check(lib().tdm_net_tiles(self.handle, _ptr(nt), _ptr(ms)))
+        return {k: (int(nt[i]), int(ms[i])) for i, k in enumerate(self.LAYER_SLOTS[:9])}
+
+    def set_tile(self, layer: str, nt: int, msub: int) -> None:
+        check(lib().tdm_net_set_tile(self.handle, self.LAYER_SLOTS.index(layer), nt, msub))
+
     def close(self):
         if self.handle:
             lib().tdm_net_destroy(self.handle)
@@ -451,6 +482,63 @@ class Pipeline:
     def close(self):
         if self.handle:
             lib().tdm_pipeline_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many fragments of uneven size through one persistent launch per stage
+    (tdm_describe_batch); with use_graph the sequence is replayed as a CUDA graph."""
+
+    def __init__(self, net: Net, max_fragments=64, max_points=20_000_000, max_keypoints=330_000,
+                 max_voxels=1_500_000_000, trunc_voxels=5.0, pad=15, use_graph=True):
+        self.net = net
+        cfg = BatchConfig(max_fragments, max_points, max_keypoints, max_voxels, trunc_voxels, pad,
+                          1 if use_graph else 0)
+        h = ctypes.c_void_p()
+        check(lib().tdm_batch_create(ctypes.byref(cfg), net.handle, ctypes.byref(h)))
+        self.handle = h
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().tdm_batch_device_bytes(self.handle))
+
+    def describe(self, pts_dev, point_offsets, voxel_sizes, keypoints, seeds, keypts=None, desc=None, stream=None):
+        """pts_dev: (sum n, 3) float32 on the device; per-fragment host lists.
+        Returns (keypts (sum k, 3), desc (sum k, 512), [Grid per fragment])."""
+        import torch
+        F = len(keypoints)
+        off = np.ascontiguousarray(point_offsets, np.int64)
+        vs = np.ascontiguousarray(voxel_sizes, np.float32)
+        ks = np.ascontiguousarray(keypoints, np.int32)
+        sd = np.ascontiguousarray(seeds, np.uint64)
+        assert off.shape == (F + 1,) and vs.shape == (F,) and sd.shape == (F,)
+        K = int(ks.sum())
+        dev = pts_dev.device
+        if keypts is None:
+            keypts = torch.empty((max(K, 1), 3), dtype=torch.float32, device=dev)
+        if desc is None:
+            desc = torch.empty((max(K, 1), 512), dtype=torch.float32, device=dev)
+        grids = (Grid * F)()
+        check(lib().tdm_describe_batch(self.handle, _ptr(pts_dev), F, _ptr(off), _ptr(vs), _ptr(ks), _ptr(sd),
+                                       _ptr(keypts), _ptr(desc), ctypes.cast(grids, ctypes.c_void_p),
+                                       _stream(stream)))
+        return keypts[:K], desc[:K], list(grids)
+
+    def stats(self):
+        n = ctypes.c_int64()
+        r = ctypes.c_int32()
+        check(lib().tdm_batch_stats(self.handle, ctypes.byref(n), ctypes.byref(r)))
+        return {"launches_per_call": n.value, "replayed": bool(r.value)}
+
+    def close(self):
+        if self.handle:
+            lib().tdm_batch_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "tdf_core.cuh"
 
 namespace tdm {
 
@@ -78,11 +79,8 @@ tdm_status grid_from_minmax(const float mn[3], const float mx[3], float vs, floa
   if (!(vs > 0.0f) || pad < 0) return fail(TDM_ERR_INVALID_ARG, "voxel_size must be > 0 and pad >= 0");
   int64_t V = 1;
   for (int a = 0; a < 3; ++a) {
-    if (!std::isfinite(mn[a]) || !std::isfinite(mx[a])) return fail(TDM_ERR_INVALID_ARG, "non-finite point coordinates");
-    float ext = roundf((mx[a] - mn[a]) / vs);
-    if (ext > 1.0e6f) return fail(TDM_ERR_INVALID_ARG, "grid extent too large");
-    g->dim[a] = (int32_t)ext + 1 + pad * 2;
-    g->origin[a] = mn[a] - (float)pad * vs + vs / 2.0f;
+    if (grid_axis(mn[a], mx[a], vs, pad, &g->dim[a], &g->origin[a]))
+      return fail(TDM_ERR_INVALID_ARG, "non-finite point coordinates or grid extent too large");
     V *= g->dim[a];
   }
   if (V >= ((int64_t)1 << 31)) return fail(TDM_ERR_INVALID_ARG, "grid has 2^31 voxels or more");

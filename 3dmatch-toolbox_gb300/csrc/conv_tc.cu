@@ -454,6 +454,11 @@ int64_t tc_tail_rows(const TcLayer& L) {
   return (int64_t)(L.nz > 1 ? 2 * L.D * L.D : 0) + slab_rows(L) + 8;
 }
 
+bool tc_layer_fits(const TcLayer& L) {
+  return L.nt > 0 && L.msub > 0 && L.cout % L.nt == 0 && 2 * L.msub * L.nt <= 512 && weight_stages(L) >= 2 &&
+         smem_bytes(L) <= kSmemLimit;
+}
+
 tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   KParams kp;
   kp.act = a.act;

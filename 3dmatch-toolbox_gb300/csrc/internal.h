@@ -62,9 +62,18 @@ struct TcArgs {
 // Rows of slack a chunk-planar input needs after its last row for layer L.
 int64_t tc_tail_rows(const TcLayer& L);
 tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s);
+// Whether layer L's (nt, msub) tile fits the shared-memory plan and TMEM.
+bool tc_layer_fits(const TcLayer& L);
 // Packs Marvin-layout weights [cout][cin][taps] (taps = nz*nyx, or the GEMM
 // K flattening for conv8) into the tcgen05 block layout; returns host bytes.
 void pack_tc_weights(const TcLayer& L, const float* w, int gemm_taps, std::vector<uint8_t>* out,
                      std::vector<float>* scales);
+
+// Net properties the batched form needs (net.cu).
+int net_max_batch(const tdm_net* net);
+tdm_precision net_precision(const tdm_net* net);
+// Changes whenever the net's workspace is reallocated or a layer's tile
+// changes: a CUDA graph holding a forward of the net is stale after that.
+uint64_t net_generation(const tdm_net* net);
 
 }  // namespace tdm

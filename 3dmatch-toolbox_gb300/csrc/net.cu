@@ -102,8 +102,12 @@ struct tdm_net {
   float act_scale[9] = {};  // FP8 form: dequantisation scale of the E4M3 input of layer l (2..7)
   bool calibrated = false;
   std::vector<void*> allocs;
+  // packed tcgen05 weights per (form, layer, N tile), filled as tiles change
+  std::map<int, uint8_t*> packed;
   uint8_t* ws = nullptr;
   size_t ws_bytes = 0;
+  // bumped whenever a buffer or tile a captured forward refers to changes
+  uint64_t generation = 0;
   int max_batch = kDefaultMaxBatch;
   // optional per-layer timing: CUDA events recorded on the launching stream
   bool timing = false;
@@ -361,7 +365,9 @@ Bf16Plan bf16_plan(const tdm_net* net, int B) {
   for (int l = 1; l < 9; ++l) {
     int64_t rows = l <= 6 ? (int64_t)B * kDin[l] * kDin[l] * kDin[l] : B;
     P.rows[l] = rows;
-    P.rows_alloc[l] = rows + tc_tail_rows(net->tc[l]);
+    int64_t tail = tc_tail_rows(net->tc[l]);
+    if (net->prec == TDM_FP8 && l <= 7) tail = std::max(tail, tc_tail_rows(net->tc8[l]));
+    P.rows_alloc[l] = rows + tail;
   }
   // buffer 0 holds inputs of l = 1, 2(pooled), 4, 6, 8; buffer 1: conv2 output (pool input), 3, 5, 7
   auto chunks = [](int l) { return kCin[l] / 8; };
@@ -497,6 +503,7 @@ tdm_status ensure_ws(tdm_net* net, size_t bytes, cudaStream_t s) {
   if (e != cudaSuccess) return cuda_status(e, "net workspace");
   net->ws = static_cast<uint8_t*>(p);
   net->ws_bytes = 0;
+  ++net->generation;
   TDM_CHECK_CUDA(cudaMemsetAsync(p, 0, bytes, s));
   net->ws_bytes = bytes;
   return TDM_OK;
@@ -674,6 +681,136 @@ extern "C" tdm_status tdm_net_layer_times(tdm_net* net, double* ms, int64_t* lau
     }
   }
   return TDM_OK;
+}
+
+namespace tdm {
+int net_max_batch(const tdm_net* net) { return net->max_batch; }
+tdm_precision net_precision(const tdm_net* net) { return net->prec; }
+uint64_t net_generation(const tdm_net* net) { return net->generation; }
+}  // namespace tdm
+
+namespace {
+
+struct Tile {
+  int nt, msub;
+};
+constexpr Tile kTiles[] = {{64, 4}, {64, 2}, {128, 2}, {128, 1}, {256, 1}};
+
+// The tcgen05 layer a forward of `net` runs for layer l.
+TcLayer& active_layer(tdm_net* net, int l) {
+  return (net->prec == TDM_FP8 && l >= 1 && l <= 7) ? net->tc8[l] : net->tc[l];
+}
+
+// Tiles layer l can run: the N tile divides cout and the plan fits; conv1's
+// im2col GEMM has one weight packing (N = 64).
+std::vector<Tile> tile_candidates(tdm_net* net, int l) {
+  std::vector<Tile> out;
+  for (const Tile& t : kTiles) {
+    TcLayer L = active_layer(net, l);
+    if (l == 0 && t.nt != 64) continue;
+    L.nt = t.nt;
+    L.msub = t.msub;
+    if (tc_layer_fits(L)) out.push_back(t);
+  }
+  return out;
+}
+
+// Switches layer l to tile t, packing its weights for t.nt once per form.
+tdm_status set_tile(tdm_net* net, int l, Tile t) {
+  TcLayer& L = active_layer(net, l);
+  const int form = (net->prec == TDM_FP8 && l >= 1 && l <= 7) ? 1 : 0;
+  auto key = [&](int nt) { return (form * 16 + l) * 1024 + nt; };
+  if (L.nt != t.nt) {
+    net->packed[key(L.nt)] = L.wpk;
+    auto it = net->packed.find(key(t.nt));
+    if (it != net->packed.end()) {
+      L.wpk = it->second;
+    } else {
+      TcLayer T = L;
+      T.nt = t.nt;
+      std::vector<uint8_t> pk;
+      std::vector<float> sc;
+      pack_tc_weights(T, net->hw[l].data(), l == 7 ? 27 : 1, &pk, &sc);
+      uint8_t* d = nullptr;
+      tdm_status st = net->upload(pk.data(), pk.size(), &d);
+      if (st) return st;
+      TDM_CHECK_CUDA(cudaDeviceSynchronize());
+      net->packed[key(t.nt)] = d;
+      L.wpk = d;
+    }
+  }
+  if (L.nt != t.nt || L.msub != t.msub) ++net->generation;
+  L.nt = t.nt;
+  L.msub = t.msub;
+  return TDM_OK;
+}
+
+}  // namespace
+
+extern "C" tdm_status tdm_net_autotune(tdm_net* net, const float* patches, int32_t b, int32_t reps, tdm_stream s) {
+  TDM_REQUIRE(net && patches && b > 0 && reps > 0, "tdm_net_autotune: bad arguments");
+  if (net->prec == TDM_FP32) return TDM_OK;  // the CUDA-core form has a single tile shape
+  TDM_REQUIRE(net->prec != TDM_FP8 || net->calibrated, "FP8 net has no activation scales yet: call tdm_net_calibrate first");
+  const int B = std::min<int>(b, net->max_batch);
+  const int nl = net->use_feat ? 9 : 8;
+  std::vector<std::vector<Tile>> cand(nl);
+  size_t rounds = 0;
+  for (int l = 0; l < nl; ++l) {
+    cand[l] = tile_candidates(net, l);
+    TDM_REQUIRE(!cand[l].empty(), "tdm_net_autotune: a layer has no tile that fits");
+    rounds = std::max(rounds, cand[l].size());
+  }
+  float* out = nullptr;
+  TDM_CHECK_CUDA(cudaMalloc(&out, (size_t)B * 512 * sizeof(float)));
+  const bool timing = net->timing;
+  net->timing = true;
+  std::vector<double> best(nl, 1e30);
+  std::vector<Tile> pick(nl);
+  tdm_status st = TDM_OK;
+  // Round r runs every layer on its r-th candidate (its first when it has
+  // fewer); per-layer CUDA events attribute the time.
+  for (size_t r = 0; r < rounds && st == TDM_OK; ++r) {
+    for (int l = 0; l < nl && st == TDM_OK; ++l) st = set_tile(net, l, cand[l][r < cand[l].size() ? r : 0]);
+    if (st) break;
+    st = net_run(net, patches, B, out, -1, s, net->prec);  // warm-up (and workspace growth)
+    if (st) break;
+    if (net->drain() != cudaSuccess) { st = fail(TDM_ERR_DEVICE, "autotune timing"); break; }
+    for (int i = 0; i < kTimedLayers; ++i) { net->layer_ms[i] = 0.0; net->layer_n[i] = 0; }
+    for (int k = 0; k < reps && st == TDM_OK; ++k) st = net_run(net, patches, B, out, -1, s, net->prec);
+    if (st) break;
+    if (net->drain() != cudaSuccess) { st = fail(TDM_ERR_DEVICE, "autotune timing"); break; }
+    for (int l = 0; l < nl; ++l) {
+      if (r >= cand[l].size()) continue;
+      if (net->layer_ms[l] < best[l]) { best[l] = net->layer_ms[l]; pick[l] = cand[l][r]; }
+    }
+  }
+  for (int l = 0; l < nl && st == TDM_OK; ++l) st = set_tile(net, l, pick[l]);
+  for (int i = 0; i < kTimedLayers; ++i) { net->layer_ms[i] = 0.0; net->layer_n[i] = 0; }
+  net->timing = timing;
+  cudaStreamSynchronize(s);
+  cudaFree(out);
+  return st;
+}
+
+extern "C" tdm_status tdm_net_tiles(const tdm_net* net, int32_t nt[9], int32_t msub[9]) {
+  TDM_REQUIRE(net && nt && msub, "tdm_net_tiles: null pointer");
+  for (int l = 0; l < 9; ++l) {
+    const TcLayer& L = (net->prec == TDM_FP8 && l >= 1 && l <= 7) ? net->tc8[l] : net->tc[l];
+    nt[l] = net->prec == TDM_FP32 ? 0 : L.nt;
+    msub[l] = net->prec == TDM_FP32 ? 0 : L.msub;
+  }
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_net_set_tile(tdm_net* net, int32_t layer, int32_t nt, int32_t msub) {
+  TDM_REQUIRE(net && layer >= 0 && layer < 9, "tdm_net_set_tile: bad arguments");
+  TDM_REQUIRE(net->prec != TDM_FP32, "tdm_net_set_tile: the FP32 form has no tile choice");
+  for (const Tile& t : tile_candidates(net, layer))
+    if (t.nt == nt && t.msub == msub) {
+      TDM_CHECK_CUDA(cudaDeviceSynchronize());  // no forward may still read the old packing's tile
+      return set_tile(net, layer, t);
+    }
+  return fail(TDM_ERR_INVALID_ARG, "tdm_net_set_tile: tile not available for this layer");
 }
 
 extern "C" tdm_status tdm_net_destroy(tdm_net* net) {

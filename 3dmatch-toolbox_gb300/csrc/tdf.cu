@@ -12,6 +12,7 @@
 #include <climits>
 
 #include "common.cuh"
+#include "tdf_core.cuh"
 
 namespace tdm {
 tdm_status grid_from_minmax(const float mn[3], const float mx[3], float vs, float trunc, int32_t pad, tdm_grid* g);
@@ -20,17 +21,6 @@ using namespace tdm;
 
 namespace {
 
-
-__device__ __forceinline__ int float_to_ordered(float f) {
-  int i = __float_as_int(f);
-  return i >= 0 ? i : i ^ 0x7FFFFFFF;
-}
-__host__ __device__ __forceinline__ float ordered_to_float(int i) {
-  int b = i >= 0 ? i : i ^ 0x7FFFFFFF;
-  float f;
-  memcpy(&f, &b, sizeof(f));
-  return f;
-}
 
 __global__ void minmax_init_kernel(int* ws) {
   if (threadIdx.x < 3) ws[threadIdx.x] = INT_MAX;
@@ -71,84 +61,26 @@ __global__ __launch_bounds__(256) void occupancy_kernel(const float* __restrict_
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float px = pts[3 * (int64_t)i], py = pts[3 * (int64_t)i + 1], pz = pts[3 * (int64_t)i + 2];
-  int gx = (int)roundf(__fdiv_rn(__fsub_rn(px, ox), vs));
-  int gy = (int)roundf(__fdiv_rn(__fsub_rn(py, oy), vs));
-  int gz = (int)roundf(__fdiv_rn(__fsub_rn(pz, oz), vs));
+  int gx = voxel_coord(px, ox, vs), gy = voxel_coord(py, oy, vs), gz = voxel_coord(pz, oz, vs);
   if (gx < 0 || gy < 0 || gz < 0 || gx >= dx || gy >= dy || gz >= dz) return;
   occ[((int64_t)gz * dy + gy) * dx + gx] = 1;
 }
 
-// Pass A, one z-plane per block row: g2[z][y][x] = min over the in-plane
-// (2r+1)^2 window of dx^2 + dy^2 over occupied voxels (kNone8 = none).  The
-// occupancy rows of a 16-row band (plus halo) are staged in shared memory,
-// scanned along x, then along y; g2 is written as bytes (it stays in L2).
-constexpr int PA_TY = 16, PA_TX = 512;
-constexpr uint8_t kNone8 = 0xFF;
-
+// Pass A (plane_tile), one tile of one z-plane per block.
 template <int R>
 __global__ __launch_bounds__(256) void tdf_plane_kernel(const uint8_t* __restrict__ occ, int dx, int dy,
                                                         uint8_t* __restrict__ g2) {
-  __shared__ uint8_t s_occ[PA_TY + 2 * R][PA_TX + 2 * R];
-  __shared__ uint8_t s_g1[PA_TY + 2 * R][PA_TX];
-  const int x0 = blockIdx.x * PA_TX, y0 = blockIdx.y * PA_TY, z = blockIdx.z;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t plane = (int64_t)dx * dy;
-  const uint8_t* src = occ + (int64_t)z * plane;
-  const int tx = min(PA_TX, dx - x0);
-  for (int ly = warp; ly < PA_TY + 2 * R; ly += 8) {
-    const int gy = y0 - R + ly;
-    const bool row_in = gy >= 0 && gy < dy;
-    for (int lx = lane; lx < tx + 2 * R; lx += 32) {
-      const int gx = x0 - R + lx;
-      s_occ[ly][lx] = (row_in && gx >= 0 && gx < dx) ? src[(int64_t)gy * dx + gx] : 0;
-    }
-  }
-  __syncthreads();
-  for (int ly = warp; ly < PA_TY + 2 * R; ly += 8)
-    for (int lx = lane; lx < tx; lx += 32) {
-      int best = kNone8;
-#pragma unroll
-      for (int d = -R; d <= R; ++d)
-        if (s_occ[ly][lx + R + d]) best = min(best, d * d);
-      s_g1[ly][lx] = (uint8_t)best;
-    }
-  __syncthreads();
-  const int ny = min(PA_TY, dy - y0);
-  uint8_t* dst = g2 + (int64_t)z * plane;
-  for (int ly = warp; ly < ny; ly += 8)
-    for (int lx = lane; lx < tx; lx += 32) {
-      int best = kNone8;
-#pragma unroll
-      for (int d = -R; d <= R; ++d) {
-        int v = s_g1[ly + R + d][lx];
-        if (v != kNone8) best = min(best, v + d * d);
-      }
-      dst[(int64_t)(y0 + ly) * dx + x0 + lx] = (uint8_t)best;
-    }
+  __shared__ PlaneSmem<R> sm;
+  plane_tile<R>(occ, dx, dy, g2, blockIdx.x * PA_TX, blockIdx.y * PA_TY, blockIdx.z, sm);
 }
 
-// Pass B: along z, then the TDF value.  Distance 0 is the voxel's own
-// occupancy, so 1 - sqrtf(0)/r = 1 reproduces the reference's "occupied -> 1".
+// Pass B (z_voxel), one voxel per thread.
 template <int R>
 __global__ __launch_bounds__(256) void tdf_z_kernel(const uint8_t* __restrict__ g2, int64_t plane, int dz,
                                                     float* __restrict__ tdf) {
   const int64_t v = (int64_t)blockIdx.x * 256 + threadIdx.x;
   if (v >= plane * dz) return;
-  const int z = (int)(v / plane);
-  int best = 0xFFFF;
-#pragma unroll
-  for (int d = -R; d <= R; ++d) {
-    const int zz = z + d;
-    if (zz < 0 || zz >= dz) continue;
-    const int g = __ldg(g2 + v + (int64_t)d * plane);
-    if (g != kNone8) best = min(best, g + d * d);
-  }
-  float out = 0.0f;
-  if (best != 0xFFFF) {
-    const float val = __fsub_rn(1.0f, __fdiv_rn(__fsqrt_rn((float)best), (float)R));
-    out = val > 0.0f ? val : 0.0f;
-  }
-  tdf[v] = out;
+  tdf[v] = z_voxel<R>(g2, plane, dz, v);
 }
 
 // The reference decodes voxel_idx through float32 (core/demo.cu:32-34); above
@@ -194,17 +126,10 @@ __global__ __launch_bounds__(256) void tdf_refcompat_kernel(const uint8_t* __res
   tdf[idx] = best;
 }
 
-__device__ __forceinline__ uint64_t mix64(uint64_t z) {
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-  return z ^ (z >> 31);
-}
-
 __global__ void keypoint_index_kernel(uint64_t seed, uint32_t n_pts, int k, int32_t* idx) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= k) return;
-  uint64_t r = mix64(seed + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ULL);
-  idx[i] = (int32_t)__umul64hi(r, (uint64_t)n_pts);
+  idx[i] = keypoint_index(seed, n_pts, i);
 }
 
 // keypts = pts[idx]; grid = round((p - o)/vs)   (core/demo.cu:168-176)
@@ -223,7 +148,7 @@ __global__ void keypoint_kernel(const float* __restrict__ pts, int n_pts, const 
   for (int a = 0; a < 3; ++a) {
     float p = pts[3 * (int64_t)j + a];
     keypts[3 * i + a] = p;
-    kp_grid[3 * i + a] = (int32_t)roundf(__fdiv_rn(__fsub_rn(p, o[a]), vs));
+    kp_grid[3 * i + a] = voxel_coord(p, o[a], vs);
   }
 }
 
@@ -232,15 +157,8 @@ __global__ __launch_bounds__(256) void gather_kernel(const float* __restrict__ t
                                                      const int32_t* __restrict__ kp_grid,
                                                      float* __restrict__ patches) {
   const int k = blockIdx.x;
-  const int bx = kp_grid[3 * k] - 15, by = kp_grid[3 * k + 1] - 15, bz = kp_grid[3 * k + 2] - 15;
-  float* out = patches + (int64_t)k * 27000;
-  for (int i = threadIdx.x; i < 27000; i += 256) {
-    int x = i % 30, y = (i / 30) % 30, z = i / 900;
-    int gx = bx + x, gy = by + y, gz = bz + z;
-    float v = 0.0f;
-    if (gx >= 0 && gy >= 0 && gz >= 0 && gx < dx && gy < dy && gz < dz) v = __ldg(tdf + ((int64_t)gz * dy + gy) * dx + gx);
-    out[i] = v;
-  }
+  gather_patch(tdf, dx, dy, dz, kp_grid[3 * k] - 15, kp_grid[3 * k + 1] - 15, kp_grid[3 * k + 2] - 15,
+               patches + (int64_t)k * 27000);
 }
 
 template <int R>

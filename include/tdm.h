@@ -133,6 +133,18 @@ tdm_status tdm_net_set_max_batch(tdm_net* net, int32_t max_batch);
  * conv1..conv8, feat; 9 = pool1); reset != 0 clears the totals. */
 tdm_status tdm_net_set_timing(tdm_net* net, int32_t enable);
 tdm_status tdm_net_layer_times(tdm_net* net, double* ms, int64_t* launches, int32_t reset);
+/* Tile autotuner (no reference counterpart: cuDNN picks its own algorithm,
+ * core/marvin.hpp:4470).  For the BF16/FP8 forms, times every (N tile,
+ * M sub-tiles) shape each tcgen05 layer can run on a forward of b patches
+ * (reps timed forwards per shape, per-layer CUDA events) and keeps the
+ * fastest per layer.  The accumulation order does not depend on the tile, so
+ * the descriptors are the same bits before and after.  No-op for FP32. */
+tdm_status tdm_net_autotune(tdm_net* net, const float* patches_dev, int32_t b, int32_t reps, tdm_stream s);
+/* Current tile per layer (0..8 = conv1..feat; 0 for the FP32 form). */
+tdm_status tdm_net_tiles(const tdm_net* net, int32_t nt[9], int32_t msub[9]);
+/* Sets one layer's tile by hand (nt in {64,128,256} dividing the layer's
+ * outputs, msub M sub-tiles of 128 rows, 2*msub*nt <= 512 TMEM columns). */
+tdm_status tdm_net_set_tile(tdm_net* net, int32_t layer, int32_t nt, int32_t msub);
 tdm_status tdm_net_destroy(tdm_net* net);
 /* Seeded He-normal weights (N(0, 2/fan_in)), uniform biases in [-0.05, 0.05],
  * written as float32 .marvin records. */
@@ -238,6 +250,47 @@ tdm_status tdm_register_pair(tdm_pipeline* p, const float* pts_a_dev, int32_t na
 /* Whole pair from host points (host->device copies inside the call). */
 tdm_status tdm_register_pair_host(tdm_pipeline* p, const float* pts_a_host, int32_t na, const float* pts_b_host,
                                   int32_t nb, uint64_t seed, int32_t k, tdm_pair_result* result, tdm_stream s);
+
+/* ---- batched description of many fragments (core/demo.cu main, run over a
+ * set of fragments at once; the reference runs demo once per fragment,
+ * evaluation/geometric-registration/getKeyptsAndDesc.m:43) -----------------
+ * Fragments of uneven point and keypoint counts and voxel sizes go through
+ * one persistent launch per stage: grids are planned on the device from each
+ * fragment's bounds (the same arithmetic as tdm_grid_from_points), and the
+ * occupancy, TDF, keypoint and gather kernels walk a device fragment table;
+ * the net runs over all patches in chunks.  With use_graph the sequence is
+ * captured as a CUDA graph on the first call for a given (points, keypoint
+ * and descriptor pointers, fragment count, total keypoints) and replayed
+ * afterwards; point counts, voxel sizes and seeds may change between
+ * replays.  Results equal tdm_describe_fragment's fragment by fragment. */
+typedef struct tdm_batch tdm_batch;
+typedef struct tdm_batch_config {
+  int32_t max_fragments; /* <= 1024 */
+  int64_t max_points;    /* over the batch */
+  int64_t max_keypoints; /* over the batch */
+  int64_t max_voxels;    /* over the batch (each grid rounded up to 256) */
+  float trunc_voxels;    /* truncation in voxels (5) for every fragment */
+  int32_t pad;           /* 15 */
+  int32_t use_graph;
+} tdm_batch_config;
+tdm_status tdm_batch_create(const tdm_batch_config* cfg, tdm_net* net, tdm_batch** out);
+tdm_status tdm_batch_destroy(tdm_batch* b);
+/* Device bytes the batch holds (arenas, table, patch chunk; the net's own
+ * workspace not included). */
+size_t tdm_batch_device_bytes(const tdm_batch* b);
+/* pts_dev: all fragments' points back to back (x,y,z float); host arrays:
+ * point_offsets[n_fragments + 1] (fragment f = points [off[f], off[f+1])),
+ * voxel_size[f], keypoints[f], seeds[f] (keypoint stream of fragment f, as
+ * tdm_keypoint_indices).  keypts_dev: sum(keypoints) x 3 float and desc_dev:
+ * sum(keypoints) x 512 float, fragment after fragment.  grids (host,
+ * n_fragments) receives each fragment's grid; may be NULL.  Returns after
+ * the stream has finished the batch. */
+tdm_status tdm_describe_batch(tdm_batch* b, const float* pts_dev, int32_t n_fragments, const int64_t* point_offsets,
+                              const float* voxel_size, const int32_t* keypoints, const uint64_t* seeds,
+                              float* keypts_dev, float* desc_dev, tdm_grid* grids, tdm_stream s);
+/* Kernel launches one call issues (counted on its first, uncaptured run) and
+ * whether the last call replayed a captured graph. */
+tdm_status tdm_batch_stats(const tdm_batch* b, int64_t* launches_per_call, int32_t* replayed);
 
 /* ---- serving: pair-registration requests of different sizes as they arrive
  * (the reference registers pairs one by one through files and MATLAB,
