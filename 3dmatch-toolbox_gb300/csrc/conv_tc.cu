@@ -381,7 +381,330 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// dx-fused form of a 3x3x3 conv with 64 BF16 inputs and 64 outputs (conv2).
+//
+// An N = 64 MMA reads its A rows (4 KB per 128 x 16) and B (2 KB) from
+// shared memory for only 128 x 64 x 16 MACs; at the SM's shared-memory rate
+// that caps it well below the tensor pipe.  Here the three dx taps of one
+// (dz, dy) share the A operand: B = [W(dz,dy,0) | W(dz,dy,1) | W(dz,dy,2)]
+// for nt output channels gives N = 3 nt, and accumulator block dx holds
+//   P_dx[r] = sum_{dz,dy} A[r + dz D^2 + dy D] . W(dz,dy,dx)
+// so output row m = P_0[m] + P_1[m + 1] + P_2[m + 2].  The epilogue takes the
+// +1 / +2 rows from the neighbouring TMEM lanes (warp shuffles, and shared
+// memory across the 32-lane quarters); a 128-row sub-tile therefore yields
+// 126 outputs.  Each CTA owns one half of the output channels (nt = 32,
+// N = 96) for all its tiles, so its 110.6 KB of weights are loaded once and
+// stay in shared memory; only the A slabs stream.
+// ---------------------------------------------------------------------------
+constexpr int kDxfNt = 32;
+constexpr int kDxfN = 3 * kDxfNt;
+constexpr int kDxfSub = 126;
+constexpr uint32_t kDxfBlock = 8u * kDxfN * 16u;       // one (dz, dy): 8 K chunks x 96 rows x 16 B
+constexpr uint32_t kDxfWBytes = 9u * kDxfBlock;         // one half's weights
+// epilogue lane exchange: per tile parity, sub-tile and lane quarter, lane 0's
+// P_1 and P_2 and lane 1's P_2 (32 channels each)
+constexpr uint32_t kDxfXchg = 2u * 2u * 4u * 96u * 4u;
+// output staging for the bulk stores: [sub-tile][chunk][128 rows][16 B]
+constexpr uint32_t kDxfStage = 2u * 4u * 128u * 16u;
+constexpr int kDxfNSA = 2;  // A slab stages
+
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+template <int MSUB, bool FP8_OUT>
+__global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams p) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr int MOUT = MSUB * kDxfSub;
+  constexpr uint32_t ACC_COLS = MSUB * kDxfN;
+  constexpr uint32_t TMEM_COLS = tmem_cols_for(2 * ACC_COLS);
+  static_assert(2 * ACC_COLS <= 512, "two accumulator buffers must fit in TMEM");
+  const int R = p.R;
+  const uint32_t a_stage = 16u * 8u * (uint32_t)R;
+  uint8_t* sW = smem;
+  uint8_t* sA = smem + kDxfWBytes;
+  float* sX = reinterpret_cast<float*>(sA + kDxfNSA * a_stage);
+  uint8_t* sO = reinterpret_cast<uint8_t*>(sX) + kDxfXchg;
+  int* sVote = reinterpret_cast<int*>(sO + kDxfStage);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sVote + 8);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * kDxfNSA + 6);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (!__syncthreads_and(aborted(p.err) ? 0 : 1)) return;
+
+  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * kDxfNSA;
+  const uint32_t wfull = emptyA + 8 * kDxfNSA, accFull = wfull + 8, accEmpty = accFull + 16, done = accEmpty + 16;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kDxfNSA; ++i) { ptx::mbar_init(fullA + 8 * i, 1); ptx::mbar_init(emptyA + 8 * i, 1); }
+    ptx::mbar_init(wfull, 1);
+    for (int i = 0; i < 2; ++i) { ptx::mbar_init(accFull + 8 * i, 1); ptx::mbar_init(accEmpty + 8 * i, 4); }
+    ptx::mbar_init(done, 1);
+    ptx::fence_barrier_init();
+    ptx::fence_proxy_async_smem();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(ptx::smem_u32(tmem_holder), TMEM_COLS);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  const uint32_t sA_u = ptx::smem_u32(sA), sW_u = ptx::smem_u32(sW);
+  const int64_t plane = (int64_t)p.D * p.D;
+  // the grid is even, so every tile t of this CTA has t % 2 == blockIdx.x % 2
+  const int half = blockIdx.x & 1;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- producer: resident weights once, then A slabs ----------------
+#ifdef TDM_WAIT_STATS
+      const long long t_loop0 = clock64();
+#endif
+      ptx::mbar_arrive_expect_tx(wfull, kDxfWBytes);
+      for (int b = 0; b < 9; ++b)
+        ptx::bulk_g2s(sW_u + b * kDxfBlock, p.wpk + (size_t)half * kDxfWBytes + (size_t)b * kDxfBlock, kDxfBlock,
+                      wfull);
+      int sa = 0;
+      uint32_t pha = 0;
+      int armedA[kDxfNSA];
+      for (int i = 0; i < kDxfNSA; ++i) armedA[i] = -1;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+        const int64_t m0 = (t >> 1) * MOUT;
+        if (!tile_has_work(p, m0, MOUT)) continue;
+        for (int zt = 0; zt < 3; ++zt) {
+          if (!TDM_TIMED_WAIT(3, wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
+          ptx::mbar_arrive_expect_tx(fullA + 8 * sa, a_stage);
+          armedA[sa] = (int)pha;
+          const uint8_t* src = p.act + (m0 + zt * plane) * 16;
+          for (int j = 0; j < 8; ++j)
+            ptx::bulk_g2s(sA_u + sa * a_stage + j * R * 16, src + j * p.act_cs, R * 16, fullA + 8 * sa);
+          if (++sa == kDxfNSA) { sa = 0; pha ^= 1; }
+        }
+        // the next tile's slabs towards L2 while this one is consumed
+        const int64_t tn = t + gridDim.x;
+        if (ok && tn < p.total_tiles) {
+          const int64_t mn = (tn >> 1) * MOUT;
+          if (tile_has_work(p, mn, MOUT))
+            for (int zt = 0; zt < 3; ++zt)
+              for (int j = 0; j < 8; ++j) ptx::bulk_prefetch_l2(p.act + (mn + zt * plane) * 16 + j * p.act_cs, R * 16);
+        }
+      }
+#ifdef TDM_WAIT_STATS
+      atomicAdd(&g_wait_stats[7], (unsigned long long)(clock64() - t_loop0));
+#endif
+      for (int i = 0; i < kDxfNSA; ++i)
+        if (armedA[i] >= 0) wait_or_flag(fullA + 8 * i, (uint32_t)armedA[i], p.err, DEV_TIMEOUT_PRODUCER);
+      wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_PRODUCER);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      constexpr uint32_t idesc = ptx::make_idesc(kDxfN, 128, 1, 1);
+      const uint32_t lboA = (uint32_t)R * 16u;
+      int sa = 0;
+      uint32_t pha = 0;
+#ifdef TDM_WAIT_STATS
+      const long long t_loop0 = clock64();
+#endif
+      bool ok = TDM_TIMED_WAIT(2, wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_MMA));
+      uint32_t j = 0;
+      for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+        const int64_t m0 = (t >> 1) * MOUT;
+        if (!tile_has_work(p, m0, MOUT)) continue;
+        const uint32_t buf = j & 1u, use = j >> 1;
+        if (!TDM_TIMED_WAIT(0, wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
+        ptx::tc_fence_after();
+        const uint32_t dbase = tmem + buf * ACC_COLS;
+        uint32_t accumulate = 0;
+        for (int zt = 0; zt < 3 && ok; ++zt) {
+          if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
+          ptx::tc_fence_after();
+          const uint32_t aBase = sA_u + sa * a_stage;
+          for (int dy = 0; dy < 3; ++dy) {
+            const uint32_t wBase = sW_u + (zt * 3 + dy) * kDxfBlock;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t bdesc = ptx::smem_desc(wBase + (2 * kk) * kDxfN * 16, kDxfN * 16, 128);
+#pragma unroll
+              for (int i = 0; i < MSUB; ++i) {
+                const uint64_t adesc =
+                    ptx::smem_desc(aBase + (2 * kk) * lboA + (uint32_t)(i * kDxfSub + dy * p.D) * 16u, lboA, 128);
+                ptx::mma_f16(dbase + i * kDxfN, adesc, bdesc, idesc, accumulate);
+              }
+              accumulate = 1;
+            }
+          }
+          ptx::mma_commit(emptyA + 8 * sa);
+          if (++sa == kDxfNSA) { sa = 0; pha ^= 1; }
+        }
+        ptx::mma_commit(accFull + 8 * buf);
+        ++j;
+      }
+      ptx::mma_commit(done);
+      wait_or_flag(done, 0, p.err, DEV_TIMEOUT_MMA);
+#ifdef TDM_WAIT_STATS
+      atomicAdd(&g_wait_stats[6], (unsigned long long)(clock64() - t_loop0));
+#endif
+    }
+  } else {
+    // ---------------- epilogue (warps 2-5, TMEM lane quarter q = warp % 4) ----------------
+    // Per tile: every quarter publishes the P_1 / P_2 values of its lanes 0
+    // and 1 (both sub-tiles) in shared memory; barrier A (which also carries
+    // the continue/stop vote and frees the output staging); outputs computed
+    // into the staging area; barrier B; then one lane per output run issues
+    // bulk shared -> global stores.  The epilogue threads themselves never
+    // store to global memory, so no barrier waits for global stores.
+    const uint32_t sO_u = ptx::smem_u32(sO);
+    constexpr int CH = FP8_OUT ? 2 : 4;  // 16-byte output chunks per row of this half
+#ifdef TDM_WAIT_STATS
+    const long long t_epi0 = clock64();
+#endif
+    const int q = warp & 3;
+    const int L = q * 32 + lane;  // TMEM lane = row within the 128-row sub-tile
+    const int64_t D3 = (int64_t)p.D * p.D * p.D;
+    const int n0 = half * kDxfNt;
+    bool issued = false;  // this lane has bulk stores in flight
+    uint32_t j = 0;
+    for (int64_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
+      const int64_t m0 = (t >> 1) * MOUT;
+      if (!tile_has_work(p, m0, MOUT)) continue;
+      const uint32_t buf = j & 1u, use = j >> 1;
+      const int got = __all_sync(
+          0xffffffffu, TDM_TIMED_WAIT(5, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE)) ? 1 : 0);
+      if (lane == 0) sVote[(j & 1u) * 4 + q] = got;
+      float* xs = sX + (j & 1u) * (MSUB * 4 * 96);
+      if (got) {
+        ptx::tc_fence_after();
+#pragma unroll
+        for (int i = 0; i < MSUB; ++i) {
+          const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + i * kDxfN;
+#pragma unroll
+          for (int c0 = 0; c0 < kDxfNt; c0 += 16) {
+            uint32_t r1[16], r2[16];
+            ptx::tmem_ld16_nowait(ta + kDxfNt + c0, r1);
+            ptx::tmem_ld16_nowait(ta + 2 * kDxfNt + c0, r2);
+            ptx::tmem_wait_ld();
+            float* xw = xs + (i * 4 + q) * 96;
+            if (lane == 0) {
+#pragma unroll
+              for (int e = 0; e < 16; ++e) { xw[c0 + e] = __uint_as_float(r1[e]); xw[32 + c0 + e] = __uint_as_float(r2[e]); }
+            } else if (lane == 1) {
+#pragma unroll
+              for (int e = 0; e < 16; ++e) xw[64 + c0 + e] = __uint_as_float(r2[e]);
+            }
+          }
+        }
+      }
+      if (issued) ptx::bulk_wait_read_all();  // the staging area is free again
+      epi_bar();  // A
+      const int* vote = sVote + (j & 1u) * 4;
+      if (!(vote[0] && vote[1] && vote[2] && vote[3])) break;
+#pragma unroll 1
+      for (int i = 0; i < MSUB; ++i) {
+        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + i * kDxfN;
+        const float* xn = xs + (i * 4 + ((q + 1) & 3)) * 96;  // next quarter (q = 3: rows >= 126 only)
+#pragma unroll 1
+        for (int c0 = 0; c0 < kDxfNt; c0 += 16) {
+          uint32_t r0[16], r1[16], r2[16];
+          ptx::tmem_ld16_nowait(ta + c0, r0);
+          ptx::tmem_ld16_nowait(ta + kDxfNt + c0, r1);
+          ptx::tmem_ld16_nowait(ta + 2 * kDxfNt + c0, r2);
+          ptx::tmem_wait_ld();
+          // neighbour-quarter values and biases: broadcast vector loads by
+          // every lane and a select, so the shuffle loop has no branches
+          float nb1[16], nb2a[16], nb2b[16], bi[16];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float4 u = reinterpret_cast<const float4*>(xn + c0)[k];
+            const float4 w = reinterpret_cast<const float4*>(xn + 32 + c0)[k];
+            const float4 z = reinterpret_cast<const float4*>(xn + 64 + c0)[k];
+            const float4 c = __ldg(reinterpret_cast<const float4*>(p.bias + n0 + c0) + k);
+            nb1[4 * k] = u.x; nb1[4 * k + 1] = u.y; nb1[4 * k + 2] = u.z; nb1[4 * k + 3] = u.w;
+            nb2a[4 * k] = w.x; nb2a[4 * k + 1] = w.y; nb2a[4 * k + 2] = w.z; nb2a[4 * k + 3] = w.w;
+            nb2b[4 * k] = z.x; nb2b[4 * k + 1] = z.y; nb2b[4 * k + 2] = z.z; nb2b[4 * k + 3] = z.w;
+            bi[4 * k] = c.x; bi[4 * k + 1] = c.y; bi[4 * k + 2] = c.z; bi[4 * k + 3] = c.w;
+          }
+          const bool l31 = lane == 31, l30 = lane == 30;
+          float v[16];
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            float s1 = __shfl_down_sync(0xffffffffu, __uint_as_float(r1[e]), 1);
+            float s2 = __shfl_down_sync(0xffffffffu, __uint_as_float(r2[e]), 2);
+            s1 = l31 ? nb1[e] : s1;
+            s2 = l31 ? nb2b[e] : (l30 ? nb2a[e] : s2);
+            const float a = ((__uint_as_float(r0[e]) + s1) + s2) + bi[e];
+            v[e] = p.relu ? fmaxf(a, 0.0f) : a;
+          }
+          // rows 126 and 127 of a sub-tile are staged too but never stored
+          if (FP8_OUT) {
+            uint4 o;
+            o.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
+            o.y = pack_e4m3x4(v[4] * p.out_qinv, v[5] * p.out_qinv, v[6] * p.out_qinv, v[7] * p.out_qinv);
+            o.z = pack_e4m3x4(v[8] * p.out_qinv, v[9] * p.out_qinv, v[10] * p.out_qinv, v[11] * p.out_qinv);
+            o.w = pack_e4m3x4(v[12] * p.out_qinv, v[13] * p.out_qinv, v[14] * p.out_qinv, v[15] * p.out_qinv);
+            *reinterpret_cast<uint4*>(sO + ((i * 4 + c0 / 16) * 128 + L) * 16) = o;
+          } else {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              uint4 o;
+              o.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
+              o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
+              o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
+              o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
+              *reinterpret_cast<uint4*>(sO + ((i * 4 + c0 / 8 + h) * 128 + L) * 16) = o;
+            }
+          }
+        }
+      }
+      ptx::tc_fence_before();
+      ptx::fence_proxy_async_smem();  // staging writes visible to the bulk copies
+      epi_bar();                      // B
+      if (lane == 0) mbar_arrive(accEmpty + 8 * buf);
+      // Output runs: sub-tile i spans rows [s, s + 126); every grid row
+      // (b, z, y) of 28 inputs holds one run of up to 26 outputs.  Lane k of
+      // quarter q = i handles the k-th grid row the sub-tile touches.
+      if (q < MSUB) {
+        const int64_t s0 = m0 + (int64_t)q * kDxfSub;
+        const int64_t e0 = min(s0 + kDxfSub, p.rows);
+        const int64_t y0 = s0 / p.D;
+        const int64_t yr = y0 + lane;  // grid row index (b*D + z)*D + y
+        const int64_t ra = max(s0, yr * p.D), rb = min(e0, yr * p.D + p.Do);
+        if (lane < 6 && ra < rb) {
+          const int64_t bz = yr / p.D;  // b*D + z
+          const int y = (int)(yr - bz * p.D);
+          const int64_t b = bz / p.D;
+          const int z = (int)(bz - b * p.D);
+          if (y < p.Do && z < p.Do) {
+            const int x = (int)(ra - yr * p.D);
+            const int64_t pout = ((b * p.Do + z) * p.Do + y) * p.Do + x;
+            const uint32_t len = (uint32_t)(rb - ra) * 16u;
+#pragma unroll
+            for (int c = 0; c < CH; ++c)
+              ptx::bulk_s2g(p.out + (int64_t)(n0 / (FP8_OUT ? 16 : 8) + c) * p.out_cs + pout * 16,
+                            sO_u + ((q * 4 + c) * 128 + (int)(ra - s0)) * 16, len);
+            ptx::bulk_commit();
+            issued = true;
+          }
+        }
+      }
+      ++j;
+    }
+    if (issued) ptx::bulk_wait_all();
+#ifdef TDM_WAIT_STATS
+    atomicAdd(&g_wait_stats[4], (unsigned long long)(clock64() - t_epi0));
+#endif
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
 int slab_rows(const TcLayer& L) {
+  if (L.dxf) return (L.msub - 1) * kDxfSub + 128 + 2 * L.D;  // exact: three stages must fit beside the weights
   int r = L.msub * 128 + (L.nyx > 1 ? 2 * L.D + 2 : 0);
   return (r + 7) & ~7;
 }
@@ -402,6 +725,7 @@ int weight_stages(const TcLayer& L) {
 }
 
 size_t smem_bytes(const TcLayer& L) {
+  if (L.dxf) return kDxfWBytes + kDxfNSA * a_stage_bytes(L) + kDxfXchg + kDxfStage + 32 + kSmemReserve;
   return NSA * a_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
 }
 
@@ -435,6 +759,23 @@ tdm_status launch_t(const KParams& kp, size_t smem, cudaStream_t s) {
   return TDM_OK;
 }
 
+template <int MSUB, bool FP8_OUT>
+tdm_status launch_dxf(const KParams& kp, size_t smem, cudaStream_t s) {
+  auto kern = tc_conv_dxf_kernel<MSUB, FP8_OUT>;
+  size_t req = std::max<size_t>(smem, 120 * 1024);
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [&] {
+    attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  });
+  if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_dxf_kernel)");
+  // an even grid keeps every CTA on one half of the output channels
+  int64_t grid = std::min<int64_t>(kp.total_tiles, sm_count() & ~1);
+  kern<<<(unsigned)std::max<int64_t>(grid, 2), kThreads, req, s>>>(kp);
+  TDM_CHECK_LAUNCH("tc_conv_dxf_kernel");
+  return TDM_OK;
+}
+
 }  // namespace
 
 #ifdef TDM_WAIT_STATS
@@ -455,6 +796,9 @@ int64_t tc_tail_rows(const TcLayer& L) {
 }
 
 bool tc_layer_fits(const TcLayer& L) {
+  if (L.dxf)
+    return L.nt == kDxfNt && (L.msub == 1 || L.msub == 2) && L.cin == 64 && L.cout == 2 * kDxfNt && L.nz == 3 &&
+           L.nyx == 9 && !L.fp8_in && smem_bytes(L) <= kSmemLimit;
   return L.nt > 0 && L.msub > 0 && L.cout % L.nt == 0 && 2 * L.msub * L.nt <= 512 && weight_stages(L) >= 2 &&
          smem_bytes(L) <= kSmemLimit;
 }
@@ -481,9 +825,23 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   kp.out_mode = L.out_mode;
   kp.relu = L.relu;
   kp.R = slab_rows(L);
-  kp.nsb = weight_stages(L);
   kp.err = device_error_word();
   if (!kp.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
+  if (L.dxf) {
+    TDM_REQUIRE(tc_layer_fits(L), "tc layer: unsupported dx-fused tile");
+    TDM_REQUIRE((reinterpret_cast<uintptr_t>(a.act) & 15) == 0 && (a.act_cs & 15) == 0 &&
+                    (reinterpret_cast<uintptr_t>(L.wpk) & 15) == 0,
+                "tc layer: operands must be 16-byte aligned");
+    if (a.rows == 0) return TDM_OK;
+    const int64_t mout = (int64_t)L.msub * kDxfSub;
+    kp.ntiles = 2;
+    kp.nsb = 0;
+    kp.total_tiles = ((a.rows + mout - 1) / mout) * 2;
+    const size_t smem = smem_bytes(L);
+    if (L.msub == 2) return L.fp8_out ? launch_dxf<2, true>(kp, smem, s) : launch_dxf<2, false>(kp, smem, s);
+    return L.fp8_out ? launch_dxf<1, true>(kp, smem, s) : launch_dxf<1, false>(kp, smem, s);
+  }
+  kp.nsb = weight_stages(L);
   TDM_REQUIRE(kp.nsb >= 2, "tc layer: shared-memory plan leaves fewer than 2 weight stages");
   TDM_REQUIRE(smem_bytes(L) <= kSmemLimit, "tc layer: shared-memory plan exceeds 227 KB");
   TDM_REQUIRE(L.cout % L.nt == 0, "tc layer: cout must be a multiple of the N tile");
@@ -511,6 +869,23 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   TDM_TC_CASE(256, 1)
 #undef TDM_TC_CASE
   return fail(TDM_ERR_UNSUPPORTED, "tc layer: unsupported (nt, msub) tile");
+}
+
+void pack_dxf_weights(const TcLayer& L, const float* w, std::vector<uint8_t>* out) {
+  out->assign((size_t)2 * kDxfWBytes, 0);
+  for (int h = 0; h < 2; ++h)
+    for (int b = 0; b < 9; ++b)  // b = dz * 3 + dy
+      for (int j = 0; j < 8; ++j)
+        for (int n = 0; n < kDxfN; ++n) {
+          const int dx = n / kDxfNt, co = h * kDxfNt + n % kDxfNt;
+          for (int e = 0; e < 8; ++e) {
+            const int ci = j * 8 + e;
+            const __nv_bfloat16 v = __float2bfloat16_rn(w[((size_t)co * L.cin + ci) * 27 + b * 3 + dx]);
+            std::memcpy(out->data() + (size_t)h * kDxfWBytes + (size_t)b * kDxfBlock + ((size_t)j * kDxfN + n) * 16 +
+                            2 * e,
+                        &v, 2);
+          }
+        }
 }
 
 // Weight blocks: for ntile, zt, cg, yx -> [chunk j][n in nt][16 bytes], where

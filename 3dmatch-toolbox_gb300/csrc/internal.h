@@ -43,6 +43,12 @@ struct TcLayer {
   int relu;
   bool fp8_in;    // operands are E4M3 (kind::f8f6f4)
   bool fp8_out;   // epilogue writes E4M3 (chunk of 16 channels per 16 bytes)
+  // dx-fused form (a 3x3x3 conv with 64 BF16 inputs and 64 outputs, i.e.
+  // conv2): the three dx taps of one (dz, dy) form a single N = 3 * nt MMA
+  // and the epilogue adds the dx = 1, 2 partial sums from the next one and
+  // two rows; nt = 32 output channels per CTA (two halves), weights resident
+  // in shared memory, msub sub-tiles of 128 rows giving 126 outputs each.
+  bool dxf = false;
   // device data
   uint8_t* wpk;   // packed weights, blocks [ntile][zt][cg][yx] of nt*128 bytes
   float* bias;    // [cout]
@@ -68,6 +74,8 @@ bool tc_layer_fits(const TcLayer& L);
 // K flattening for conv8) into the tcgen05 block layout; returns host bytes.
 void pack_tc_weights(const TcLayer& L, const float* w, int gemm_taps, std::vector<uint8_t>* out,
                      std::vector<float>* scales);
+// Weights of a dx-fused layer: [half][dz*3+dy][chunk][dx*nt + c][16 bytes].
+void pack_dxf_weights(const TcLayer& L, const float* w, std::vector<uint8_t>* out);
 
 // Net properties the batched form needs (net.cu).
 int net_max_batch(const tdm_net* net);

@@ -198,6 +198,11 @@ TcLayer make_tc_layer(int l, bool use_feat) {
   if (L.cout == 64) { L.nt = 64; L.msub = 4; }
   else if (L.cout == 128) { L.nt = 128; L.msub = 2; }
   else { L.nt = 256; L.msub = 1; }
+  if (l == 1) {  // conv2: the dx taps share one N = 96 MMA per half of the outputs
+    L.dxf = true;
+    L.nt = 32;
+    L.msub = 2;
+  }
   return L;
 }
 
@@ -255,7 +260,8 @@ tdm_status setup_weights(tdm_net* net) {
       TcLayer L = make_tc_layer(l, net->use_feat != 0);
       std::vector<uint8_t> pk;
       std::vector<float> sc;
-      pack_tc_weights(L, net->hw[l].data(), l == 7 ? 27 : 1, &pk, &sc);
+      if (L.dxf) pack_dxf_weights(L, net->hw[l].data(), &pk);
+      else pack_tc_weights(L, net->hw[l].data(), l == 7 ? 27 : 1, &pk, &sc);
       st = net->upload(pk.data(), pk.size(), &L.wpk);
       if (st != TDM_OK) return st;
       L.bias = net->d_b[l];
@@ -705,6 +711,14 @@ TcLayer& active_layer(tdm_net* net, int l) {
 // im2col GEMM has one weight packing (N = 64).
 std::vector<Tile> tile_candidates(tdm_net* net, int l) {
   std::vector<Tile> out;
+  if (active_layer(net, l).dxf) {  // the dx-fused conv2: 32 channels per CTA, 1 or 2 sub-tiles
+    for (int ms : {2, 1}) {
+      TcLayer L = active_layer(net, l);
+      L.msub = ms;
+      if (tc_layer_fits(L)) out.push_back(Tile{32, ms});
+    }
+    return out;
+  }
   for (const Tile& t : kTiles) {
     TcLayer L = active_layer(net, l);
     if (l == 0 && t.nt != 64) continue;
