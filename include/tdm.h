@@ -77,7 +77,8 @@ tdm_status tdm_grid_from_points(const float* pts_dev, int32_t n, float voxel_siz
                                 tdm_grid* grid_out, void* ws_dev, tdm_stream s);
 /* TDF of core/demo.cu:22-57 over the whole grid: occupancy scatter of the
  * points, exact windowed squared distance, 1 - d/trunc.  tdf_dev: V floats.
- * ws_dev: tdm_tdf_workspace_bytes(grid) bytes (occupancy). */
+ * ws_dev: tdm_tdf_workspace_bytes(grid) = 2 V bytes (occupancy, then the
+ * in-plane squared distances). */
 size_t tdm_tdf_workspace_bytes(const tdm_grid* grid);
 tdm_status tdm_tdf(const float* pts_dev, int32_t n, const tdm_grid* grid, int32_t decode_mode, float* tdf_dev,
                    void* ws_dev, size_t ws_bytes, tdm_stream s);
