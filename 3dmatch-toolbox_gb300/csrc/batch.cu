@@ -42,8 +42,9 @@ struct FragGeo {  // plan-kernel output
 };
 
 struct Totals {
-  int64_t voxels;  // arena voxels in use (grids rounded up to 256)
+  int64_t voxels;  // arena voxels in use (pitched grids rounded up to 256)
   int64_t tiles;   // in-plane pass tiles
+  int64_t rows;    // z-pass warp work items
   int64_t points;
   int32_t status;  // 0, kCapacity or kGeometry
   int32_t bad_fragment;
@@ -118,9 +119,9 @@ __global__ __launch_bounds__(256) void minmax_kernel(const float* __restrict__ p
 // and plane-tile offsets, capacity check.  One block.
 __global__ void plan_kernel(int F, const FragIn* __restrict__ in, const int* __restrict__ mm, int32_t pad,
                             int64_t cap_voxels, FragGeo* __restrict__ geo, int64_t* __restrict__ vox_bound,
-                            int64_t* __restrict__ tile_bound, const int64_t* __restrict__ pt_bound,
-                            Totals* __restrict__ tot) {
-  __shared__ int64_t sV[kMaxFragments], sT[kMaxFragments];
+                            int64_t* __restrict__ tile_bound, int64_t* __restrict__ row_bound,
+                            const int64_t* __restrict__ pt_bound, Totals* __restrict__ tot) {
+  __shared__ int64_t sV[kMaxFragments], sT[kMaxFragments], sR[kMaxFragments];
   __shared__ int s_bad;
   if (threadIdx.x == 0) s_bad = INT_MAX;
   __syncthreads();
@@ -140,21 +141,26 @@ __global__ void plan_kernel(int F, const FragIn* __restrict__ in, const int* __r
       g.dim[0] = g.dim[1] = g.dim[2] = 0;
     }
     geo[f] = g;
-    sV[f] = (V + 255) / 256 * 256;
-    sT[f] = err ? 0 : (int64_t)((g.dim[0] + PA_TX - 1) / PA_TX) * ((g.dim[1] + PA_TY - 1) / PA_TY) * g.dim[2];
+    const int64_t PV = err ? 0 : occ_pitch(g.dim[0]) * g.dim[1] * g.dim[2];
+    sV[f] = (PV + 255) / 256 * 256;
+    sT[f] = err ? 0 : (int64_t)((g.dim[0] + PB_TX - 1) / PB_TX) * ((g.dim[1] + PB_TY - 1) / PB_TY) * g.dim[2];
+    sR[f] = err ? 0 : (int64_t)g.dim[1] * ((g.dim[0] + 127) / 128) * ((g.dim[2] + kZChunk - 1) / kZChunk);
   }
   __syncthreads();
   if (threadIdx.x != 0) return;
-  int64_t v = 0, t = 0;
+  int64_t v = 0, t = 0, rw = 0;
   for (int f = 0; f < F; ++f) {
     vox_bound[f] = v;
     tile_bound[f] = t;
+    row_bound[f] = rw;
     geo[f].vox_off = v;
     v += sV[f];
     t += sT[f];
+    rw += sR[f];
   }
   vox_bound[F] = v;
   tile_bound[F] = t;
+  row_bound[F] = rw;
   Totals r{};
   r.bad_fragment = -1;
   if (s_bad != INT_MAX) {
@@ -165,6 +171,7 @@ __global__ void plan_kernel(int F, const FragIn* __restrict__ in, const int* __r
   } else {
     r.voxels = v;
     r.tiles = t;
+    r.rows = rw;
     r.points = pt_bound[F];
   }
   *tot = r;
@@ -177,7 +184,7 @@ __global__ __launch_bounds__(256) void zero_kernel(uint8_t* __restrict__ occ, co
     p[i] = make_uint4(0, 0, 0, 0);
 }
 
-// occ[vox_off + (z*dy + y)*dx + x] = 1 for every point (core/demo.cu:127-135)
+// occ[vox_off + (z*dy + y)*X + x] = 1 for every point (core/demo.cu:127-135; X = occ_pitch(dx))
 __global__ __launch_bounds__(256) void occupancy_kernel(const float* __restrict__ pts, int F,
                                                         const int64_t* __restrict__ pt_bound,
                                                         const FragIn* __restrict__ in, const FragGeo* __restrict__ geo,
@@ -194,7 +201,7 @@ __global__ __launch_bounds__(256) void occupancy_kernel(const float* __restrict_
     const int gy = voxel_coord(pts[3 * i + 1], g.origin[1], vs);
     const int gz = voxel_coord(pts[3 * i + 2], g.origin[2], vs);
     if (gx < 0 || gy < 0 || gz < 0 || gx >= g.dim[0] || gy >= g.dim[1] || gz >= g.dim[2]) continue;
-    occ[g.vox_off + ((int64_t)gz * g.dim[1] + gy) * g.dim[0] + gx] = 1;
+    occ[g.vox_off + ((int64_t)gz * g.dim[1] + gy) * occ_pitch(g.dim[0]) + gx] = 1;
   }
 }
 
@@ -211,32 +218,41 @@ __global__ __launch_bounds__(256) void plane_kernel(const uint8_t* __restrict__ 
   for (int64_t t = blockIdx.x; t < n; t += gridDim.x) {
     const int f = find_frag(sb, F, t);
     const FragGeo g = geo[f];
-    const int ntx = (g.dim[0] + PA_TX - 1) / PA_TX, nty = (g.dim[1] + PA_TY - 1) / PA_TY;
+    const int ntx = (g.dim[0] + PB_TX - 1) / PB_TX, nty = (g.dim[1] + PB_TY - 1) / PB_TY;
     const int64_t local = t - sb[f];
     const int z = (int)(local / ((int64_t)ntx * nty));
     const int rem = (int)(local - (int64_t)z * ntx * nty);
-    plane_tile<R>(occ + g.vox_off, g.dim[0], g.dim[1], g2 + g.vox_off, (rem % ntx) * PA_TX, (rem / ntx) * PA_TY, z,
+    plane_tile<R>(occ + g.vox_off, g.dim[0], g.dim[1], g2 + g.vox_off, (rem % ntx) * PB_TX, (rem / ntx) * PB_TY, z,
                   sm);
     __syncthreads();
   }
 }
 
-// Pass along z and the TDF value of every voxel of every grid (z_voxel).
+// Pass along z of every grid (z_column): warp work items (y, 128-voxel x
+// segment, 32-step z chunk) numbered fragment after fragment.
+constexpr int kZThreads = 128;
 template <int R>
-__global__ __launch_bounds__(256) void z_kernel(const uint8_t* __restrict__ g2, float* __restrict__ tdf, int F,
-                                                const int64_t* __restrict__ vox_bound, const FragGeo* __restrict__ geo,
-                                                const Totals* __restrict__ tot) {
+__global__ __launch_bounds__(kZThreads) void z_kernel(const uint8_t* __restrict__ g2, float* __restrict__ tdf, int F,
+                                                      const int64_t* __restrict__ item_bound,
+                                                      const FragGeo* __restrict__ geo, const Totals* __restrict__ tot) {
   __shared__ int64_t sb[kMaxFragments + 1];
-  for (int i = threadIdx.x; i <= F; i += blockDim.x) sb[i] = vox_bound[i];
+  __shared__ float lut[256];
+  __shared__ float s_w[kZThreads / 32][128];
+  for (int i = threadIdx.x; i <= F; i += blockDim.x) sb[i] = item_bound[i];
+  tdf_lut<R>(lut);
   __syncthreads();
-  const int64_t n = tot->voxels;
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const int f = find_frag(sb, F, v);
+  const int64_t n = tot->rows;
+  const int w = threadIdx.x >> 5;
+  for (int64_t it = (int64_t)blockIdx.x * (kZThreads / 32) + w; it < n; it += (int64_t)gridDim.x * (kZThreads / 32)) {
+    const int f = find_frag(sb, F, it);
     const FragGeo g = geo[f];
-    const int64_t plane = (int64_t)g.dim[0] * g.dim[1];
-    const int64_t local = v - sb[f];
-    if (local >= plane * g.dim[2]) continue;  // rounding gap between grids
-    tdf[v] = z_voxel<R>(g2 + g.vox_off, plane, g.dim[2], local);
+    const int nseg = (g.dim[0] + 127) / 128, nzc = (g.dim[2] + kZChunk - 1) / kZChunk;
+    const int64_t local = it - sb[f];
+    const int zc = (int)(local % nzc);
+    const int64_t r = local / nzc;
+    const int seg = (int)(r % nseg), y = (int)(r / nseg);
+    z_column<R>(g2 + g.vox_off, g.dim[0], g.dim[1], g.dim[2], y, seg * 128, zc * kZChunk,
+                min(g.dim[2], (zc + 1) * kZChunk), lut, s_w[w], tdf + g.vox_off);
   }
 }
 
@@ -282,9 +298,9 @@ __global__ __launch_bounds__(256) void gather_kernel(const float* __restrict__ t
 
 template <int R>
 void launch_tdf_passes(const uint8_t* occ, uint8_t* g2, float* tdf, int F, const int64_t* tile_bound,
-                       const int64_t* vox_bound, const FragGeo* geo, const Totals* tot, int sms, cudaStream_t s) {
+                       const int64_t* row_bound, const FragGeo* geo, const Totals* tot, int sms, cudaStream_t s) {
   plane_kernel<R><<<sms * 8, 256, 0, s>>>(occ, g2, F, tile_bound, geo, tot);
-  z_kernel<R><<<sms * 8, 256, 0, s>>>(g2, tdf, F, vox_bound, geo, tot);
+  z_kernel<R><<<sms * 16, kZThreads, 0, s>>>(g2, tdf, F, row_bound, geo, tot);
 }
 
 }  // namespace
@@ -309,7 +325,7 @@ struct tdm_batch {
   uint8_t* up = nullptr;
   uint8_t* down = nullptr;
   // table layout (bytes), fixed by max_fragments
-  size_t o_in, o_ptb, o_kpb, up_bytes, o_geo, o_voxb, o_tileb, o_mm, o_tot, down_bytes, table_bytes;
+  size_t o_in, o_ptb, o_kpb, up_bytes, o_geo, o_voxb, o_tileb, o_rowb, o_mm, o_tot, down_bytes, table_bytes;
   // captured graph; capture runs on a private stream (the legacy default
   // stream cannot be captured), replays on the caller's
   cudaStream_t cap = nullptr;
@@ -334,6 +350,7 @@ struct tdm_batch {
   FragGeo* d_geo() const { return reinterpret_cast<FragGeo*>(table + o_geo); }
   int64_t* d_voxb() const { return reinterpret_cast<int64_t*>(table + o_voxb); }
   int64_t* d_tileb() const { return reinterpret_cast<int64_t*>(table + o_tileb); }
+  int64_t* d_rowb() const { return reinterpret_cast<int64_t*>(table + o_rowb); }
   int* d_mm() const { return reinterpret_cast<int*>(table + o_mm); }
   Totals* d_tot() const { return reinterpret_cast<Totals*>(table + o_tot); }
 };
@@ -355,7 +372,7 @@ tdm_status run_sequence(tdm_batch* b, const float* pts, int F, int64_t total_k, 
   reset_kernel<<<1, 256, 0, s>>>(F, b->d_mm(), b->d_tot());
   minmax_kernel<<<g, 256, 0, s>>>(pts, F, b->d_ptb(), b->d_mm());
   plan_kernel<<<1, 1024, 0, s>>>(F, b->d_in(), b->d_mm(), b->cfg.pad, b->cfg.max_voxels, b->d_geo(), b->d_voxb(),
-                                 b->d_tileb(), b->d_ptb(), b->d_tot());
+                                 b->d_tileb(), b->d_rowb(), b->d_ptb(), b->d_tot());
   zero_kernel<<<g, 256, 0, s>>>(b->occ, b->d_tot());
   occupancy_kernel<<<g, 256, 0, s>>>(pts, F, b->d_ptb(), b->d_in(), b->d_geo(), b->d_tot(), b->occ);
   note_launches(4);
@@ -363,7 +380,7 @@ tdm_status run_sequence(tdm_batch* b, const float* pts, int F, int64_t total_k, 
   uint8_t* g2 = b->occ + b->cfg.max_voxels;
   switch (b->R) {
 #define TDM_R_CASE(R_) \
-  case R_: launch_tdf_passes<R_>(b->occ, g2, b->tdf, F, b->d_tileb(), b->d_voxb(), b->d_geo(), b->d_tot(), b->sms, s); break;
+  case R_: launch_tdf_passes<R_>(b->occ, g2, b->tdf, F, b->d_tileb(), b->d_rowb(), b->d_geo(), b->d_tot(), b->sms, s); break;
     TDM_R_CASE(1) TDM_R_CASE(2) TDM_R_CASE(3) TDM_R_CASE(4) TDM_R_CASE(5)
     TDM_R_CASE(6) TDM_R_CASE(7) TDM_R_CASE(8) TDM_R_CASE(9) TDM_R_CASE(10)
 #undef TDM_R_CASE
@@ -415,7 +432,8 @@ extern "C" tdm_status tdm_batch_create(const tdm_batch_config* cfg, tdm_net* net
   b->down_bytes = b->o_tot + sizeof(Totals) - b->o_geo;
   b->o_voxb = al(b->o_tot + sizeof(Totals));
   b->o_tileb = al(b->o_voxb + (F + 1) * 8);
-  b->o_mm = al(b->o_tileb + (F + 1) * 8);
+  b->o_rowb = al(b->o_tileb + (F + 1) * 8);
+  b->o_mm = al(b->o_rowb + (F + 1) * 8);
   b->table_bytes = al(b->o_mm + 6 * F * 4);
   tdm_status st = batch_alloc((void**)&b->table, b->table_bytes, &b->device_bytes);
   if (!st) st = batch_alloc((void**)&b->occ, 2 * (size_t)b->cfg.max_voxels, &b->device_bytes);

@@ -77,6 +77,10 @@ void pack_tc_weights(const TcLayer& L, const float* w, int gemm_taps, std::vecto
 // Weights of a dx-fused layer: [half][dz*3+dy][chunk][dx*nt + c][16 bytes].
 void pack_dxf_weights(const TcLayer& L, const float* w, std::vector<uint8_t>* out);
 
+// TDF workspace bytes enough for any grid of at most V voxels: the x rows of
+// the two byte arrays are padded to 4 and a grid is at least 31 voxels wide.
+inline size_t tdf_workspace_cap(int64_t V) { return 2 * ((size_t)V * 34 / 31 + 1024); }
+
 // Net properties the batched form needs (net.cu).
 int net_max_batch(const tdm_net* net);
 tdm_precision net_precision(const tdm_net* net);

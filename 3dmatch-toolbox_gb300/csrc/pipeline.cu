@@ -67,7 +67,7 @@ extern "C" tdm_status tdm_pipeline_create(const tdm_pipeline_config* cfg, tdm_ne
     if (!st) st = p->alloc(&p->kpg[f], K * 12);
     if (!st) st = p->alloc(&p->tdf[f], V * 4);
   }
-  if (!st) st = p->alloc(&p->occ, 2 * V);  // occupancy + in-plane distances (tdm_tdf_workspace_bytes)
+  if (!st) st = p->alloc(&p->occ, tdf_workspace_cap(V));  // occupancy + in-plane distances
   if (!st) st = p->alloc(&p->grid_ws, tdm_grid_workspace_bytes());
   if (!st) st = p->alloc(&p->patches, 2 * K * 27000 * 4);
   if (!st) st = p->alloc(&p->desc, 2 * K * 512 * 4);
@@ -108,7 +108,7 @@ tdm_status fragment_front(tdm_pipeline* p, int f, const float* pts, int32_t n, c
                           int32_t k, float* keypts, float* patches, cudaStream_t s) {
   TDM_REQUIRE((int64_t)g.dim[0] * g.dim[1] * g.dim[2] <= p->cfg.max_voxels,
               "fragment grid exceeds the pipeline's max_voxels");
-  tdm_status st = tdm_tdf(pts, n, &g, TDM_TDF_EXACT, p->tdf[f], p->occ, 2 * (size_t)p->cfg.max_voxels, s);
+  tdm_status st = tdm_tdf(pts, n, &g, TDM_TDF_EXACT, p->tdf[f], p->occ, tdf_workspace_cap(p->cfg.max_voxels), s);
   if (st) return st;
   st = tdm_keypoint_indices(seed, n, k, p->idx[f], s);
   if (st) return st;

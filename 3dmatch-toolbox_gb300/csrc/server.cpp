@@ -23,6 +23,7 @@
 #include <thread>
 #include <vector>
 
+#include "internal.h"
 #include "tdm.h"
 
 namespace tdm {
@@ -104,7 +105,8 @@ struct tdm_server {
 static size_t slot_footprint(const tdm_server_config& c, const tdm_net* net) {
   const size_t K = (size_t)c.pipeline.max_keypoints, N = (size_t)c.pipeline.max_points,
                V = (size_t)c.pipeline.max_voxels;
-  size_t bytes = 2 * (N * 12 + K * 28 + V * 4) + 2 * V + 2 * K * 27000 * 4 + 2 * K * 512 * 4;
+  size_t bytes = 2 * (N * 12 + K * 28 + V * 4) + tdm::tdf_workspace_cap((int64_t)V) + 2 * K * 27000 * 4 +
+                 2 * K * 512 * 4;
   bytes += tdm_mnn_workspace_bytes((int)K, (int)K, 512) + K * 40;
   bytes += tdm_ransac_workspace_bytes((int)K, c.pipeline.ransac.iterations);
   bytes += tdm_net_workspace_bytes(net, (int32_t)(2 * K));

@@ -9,6 +9,7 @@
 // Because sqrtf, /r and 1-x are monotone, 1 - sqrtf(g3)/r equals the
 // reference's running max of 1 - sqrtf(d^2)/r bit for bit (integer d^2 is
 // exact in float; sqrtf and the division are IEEE round-to-nearest).
+#include <algorithm>
 #include <climits>
 
 #include "common.cuh"
@@ -54,7 +55,7 @@ __global__ __launch_bounds__(256) void minmax_kernel(const float* __restrict__ p
   }
 }
 
-// occ[z*dy*dx + y*dx + x] = 1, x = round((p - o)/vs)   (core/demo.cu:127-135)
+// occ[(z*dy + y)*X + x] = 1, x = round((p - o)/vs)   (core/demo.cu:127-135; X = occ_pitch(dx))
 __global__ __launch_bounds__(256) void occupancy_kernel(const float* __restrict__ pts, int n, int dx, int dy, int dz,
                                                         float ox, float oy, float oz, float vs,
                                                         uint8_t* __restrict__ occ) {
@@ -63,7 +64,7 @@ __global__ __launch_bounds__(256) void occupancy_kernel(const float* __restrict_
   float px = pts[3 * (int64_t)i], py = pts[3 * (int64_t)i + 1], pz = pts[3 * (int64_t)i + 2];
   int gx = voxel_coord(px, ox, vs), gy = voxel_coord(py, oy, vs), gz = voxel_coord(pz, oz, vs);
   if (gx < 0 || gy < 0 || gz < 0 || gx >= dx || gy >= dy || gz >= dz) return;
-  occ[((int64_t)gz * dy + gy) * dx + gx] = 1;
+  occ[((int64_t)gz * dy + gy) * occ_pitch(dx) + gx] = 1;
 }
 
 // Pass A (plane_tile), one tile of one z-plane per block.
@@ -71,16 +72,39 @@ template <int R>
 __global__ __launch_bounds__(256) void tdf_plane_kernel(const uint8_t* __restrict__ occ, int dx, int dy,
                                                         uint8_t* __restrict__ g2) {
   __shared__ PlaneSmem<R> sm;
-  plane_tile<R>(occ, dx, dy, g2, blockIdx.x * PA_TX, blockIdx.y * PA_TY, blockIdx.z, sm);
+  plane_tile<R>(occ, dx, dy, g2, blockIdx.x * PB_TX, blockIdx.y * PB_TY, blockIdx.z, sm);
 }
 
-// Pass B (z_voxel), one voxel per thread.
+// Pass B (z_column): a warp work item is (y, 128-voxel x segment, 32-step z
+// chunk); blocks of 4 warps walk the items.
+constexpr int kZThreads = 128;
 template <int R>
-__global__ __launch_bounds__(256) void tdf_z_kernel(const uint8_t* __restrict__ g2, int64_t plane, int dz,
-                                                    float* __restrict__ tdf) {
-  const int64_t v = (int64_t)blockIdx.x * 256 + threadIdx.x;
-  if (v >= plane * dz) return;
-  tdf[v] = z_voxel<R>(g2, plane, dz, v);
+__global__ __launch_bounds__(kZThreads) void tdf_z_kernel(const uint8_t* __restrict__ g2, int dx, int dy, int dz,
+                                                          float* __restrict__ tdf) {
+  __shared__ float lut[256];
+  __shared__ float s_w[kZThreads / 32][128];
+  tdf_lut<R>(lut);
+  __syncthreads();
+  const int nseg = (dx + 127) / 128, nzc = (dz + kZChunk - 1) / kZChunk;
+  const int64_t items = (int64_t)dy * nseg * nzc;
+  const int w = threadIdx.x >> 5;
+  for (int64_t it = (int64_t)blockIdx.x * (kZThreads / 32) + w; it < items; it += (int64_t)gridDim.x * (kZThreads / 32)) {
+    const int zc = (int)(it % nzc);
+    const int64_t r = it / nzc;
+    const int seg = (int)(r % nseg), y = (int)(r / nseg);
+    z_column<R>(g2, dx, dy, dz, y, seg * 128, zc * kZChunk, min(dz, (zc + 1) * kZChunk), lut, s_w[w], tdf);
+  }
+}
+
+int z_blocks() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 148;
+    n = sms * 16;
+  }
+  return n;
 }
 
 // The reference decodes voxel_idx through float32 (core/demo.cu:32-34); above
@@ -110,7 +134,8 @@ __global__ __launch_bounds__(256) void tdf_refcompat_kernel(const uint8_t* __res
   int ex = (int)(idx - (int64_t)ez * plane - (int64_t)ey * dx);
   int x, y, z;
   refcompat_decode(idx, dx, dy, mode, x, y, z);
-  if ((x == ex && y == ey && z == ez) || occ[idx]) return;
+  const int64_t X = occ_pitch(dx);
+  if ((x == ex && y == ey && z == ez) || occ[((int64_t)ez * dy + ey) * X + ex]) return;
   float best = 0.0f;
   int xa = max(0, x - r), xb = min(dx, x + r + 1);
   int ya = max(0, y - r), yb = min(dy, y + r + 1);
@@ -118,7 +143,7 @@ __global__ __launch_bounds__(256) void tdf_refcompat_kernel(const uint8_t* __res
   for (int iz = za; iz < zb; ++iz)
     for (int iy = ya; iy < yb; ++iy)
       for (int ix = xa; ix < xb; ++ix)
-        if (occ[((int64_t)iz * dy + iy) * dx + ix]) {
+        if (occ[((int64_t)iz * dy + iy) * X + ix]) {
           int d2 = (x - ix) * (x - ix) + (y - iy) * (y - iy) + (z - iz) * (z - iz);
           float v = __fsub_rn(1.0f, __fdiv_rn(__fsqrt_rn((float)d2), (float)r));
           if (v > best) best = v;
@@ -163,12 +188,15 @@ __global__ __launch_bounds__(256) void gather_kernel(const float* __restrict__ t
 
 template <int R>
 void launch_tdf(const uint8_t* occ, uint8_t* g2, const tdm_grid* g, float* tdf, cudaStream_t s) {
-  dim3 ga((g->dim[0] + PA_TX - 1) / PA_TX, (g->dim[1] + PA_TY - 1) / PA_TY, g->dim[2]);
+  dim3 ga((g->dim[0] + PB_TX - 1) / PB_TX, (g->dim[1] + PB_TY - 1) / PB_TY, g->dim[2]);
   tdf_plane_kernel<R><<<ga, 256, 0, s>>>(occ, g->dim[0], g->dim[1], g2);
-  const int64_t plane = (int64_t)g->dim[0] * g->dim[1];
-  const int64_t V = plane * g->dim[2];
-  tdf_z_kernel<R><<<(unsigned)((V + 255) / 256), 256, 0, s>>>(g2, plane, g->dim[2], tdf);
+  const int64_t items = (int64_t)g->dim[1] * ((g->dim[0] + 127) / 128) * ((g->dim[2] + kZChunk - 1) / kZChunk);
+  const int64_t blocks = std::min<int64_t>((items + kZThreads / 32 - 1) / (kZThreads / 32), z_blocks());
+  tdf_z_kernel<R><<<(unsigned)blocks, kZThreads, 0, s>>>(g2, g->dim[0], g->dim[1], g->dim[2], tdf);
 }
+
+// bytes of the pitched occupancy (and of the pitched in-plane array)
+size_t pitched_voxels(const tdm_grid* g) { return (size_t)occ_pitch(g->dim[0]) * g->dim[1] * g->dim[2]; }
 
 int search_radius(const tdm_grid* g) { return (int)roundf(g->trunc_margin / g->voxel_size); }
 
@@ -199,8 +227,8 @@ extern "C" tdm_status tdm_grid_from_points(const float* pts, int32_t n, float vs
 
 extern "C" size_t tdm_tdf_workspace_bytes(const tdm_grid* g) {
   if (!g) return 0;
-  // occupancy bytes + in-plane squared distances (bytes)
-  return 2 * (size_t)g->dim[0] * g->dim[1] * g->dim[2];
+  // occupancy + in-plane squared distances, bytes, x rows padded to 4
+  return 2 * pitched_voxels(g);
 }
 
 extern "C" tdm_status tdm_tdf(const float* pts, int32_t n, const tdm_grid* g, int32_t mode, float* tdf, void* ws,
@@ -211,9 +239,10 @@ extern "C" tdm_status tdm_tdf(const float* pts, int32_t n, const tdm_grid* g, in
   TDM_REQUIRE(V > 0 && ws_bytes >= tdm_tdf_workspace_bytes(g), "tdm_tdf: workspace too small");
   int r = search_radius(g);
   TDM_REQUIRE(r >= 1 && r <= 10, "tdm_tdf: trunc_margin/voxel_size must round to 1..10 voxels");
+  const size_t PV = pitched_voxels(g);
   uint8_t* occ = static_cast<uint8_t*>(ws);
-  uint8_t* g2 = occ + V;
-  TDM_CHECK_CUDA(cudaMemsetAsync(occ, 0, V, s));
+  uint8_t* g2 = occ + PV;
+  TDM_CHECK_CUDA(cudaMemsetAsync(occ, 0, PV, s));
   occupancy_kernel<<<(n + 255) / 256, 256, 0, s>>>(pts, n, g->dim[0], g->dim[1], g->dim[2], g->origin[0],
                                                    g->origin[1], g->origin[2], g->voxel_size, occ);
   TDM_CHECK_LAUNCH("occupancy_kernel");

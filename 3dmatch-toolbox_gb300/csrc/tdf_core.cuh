@@ -44,76 +44,133 @@ __device__ __forceinline__ int voxel_coord(float p, float o, float vs) {
   return (int)roundf(__fdiv_rn(__fsub_rn(p, o), vs));
 }
 
-// In-plane pass of the separable TDF on one tile of one z-plane:
-// g2[z][y][x] = min over the in-plane (2R+1)^2 window of dx^2 + dy^2 over
-// occupied voxels (kNone8 = none).  The occupancy rows of a PA_TY-row band
-// (plus halo) are staged in shared memory, scanned along x, then along y.
-// 256 threads; the caller synchronises before reusing the shared arrays.
-constexpr int PA_TY = 16, PA_TX = 512;
+// The occupancy and in-plane distance arrays are stored with each x row
+// padded to a multiple of 4 bytes (pitch X = occ_pitch(dx), index
+// (z*dy + y)*X + x, padding bytes zero), so 4 voxels of a row are one aligned
+// 32-bit word.  Squared distances are bytes: in-plane values are <= 2 R^2 <=
+// 200, "none" is 0xFF, and sums saturate at 0xFF (__vaddus4), which maps every
+// distance above R^2 to the same value 0 as the reference.
+__host__ __device__ inline int64_t occ_pitch(int dx) { return ((int64_t)dx + 3) & ~(int64_t)3; }
+
+constexpr int PB_TX = 128, PB_TY = 16;  // in-plane tile: 128 x positions, 16 rows
+constexpr int PB_HALO = 12;             // staged bytes left of the tile (>= R, multiple of 4)
 constexpr uint8_t kNone8 = 0xFF;
 
 template <int R>
 struct PlaneSmem {
-  uint8_t occ[PA_TY + 2 * R][PA_TX + 2 * R];
-  uint8_t g1[PA_TY + 2 * R][PA_TX];
+  uint32_t occ[PB_TY + 2 * R][(PB_TX + 2 * PB_HALO) / 4];  // byte j of a row <-> x0 - PB_HALO + j
+  uint32_t g1[PB_TY + 2 * R][PB_TX / 4];
 };
 
+// In-plane pass on one tile of one z-plane (256 threads):
+//   g1 = min_{|dx|<=R, occ} dx^2 along x (a 28-bit occupancy mask per 4
+//        positions, nearest set bit on either side),
+//   g2 = min_{|dy|<=R} dy^2 + g1 along y (four bytes at a time).
 template <int R>
 __device__ __forceinline__ void plane_tile(const uint8_t* __restrict__ occ, int dx, int dy, uint8_t* __restrict__ g2,
                                            int x0, int y0, int z, PlaneSmem<R>& sm) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t plane = (int64_t)dx * dy;
-  const uint8_t* src = occ + (int64_t)z * plane;
-  const int tx = min(PA_TX, dx - x0);
-  for (int ly = warp; ly < PA_TY + 2 * R; ly += 8) {
-    const int gy = y0 - R + ly;
-    const bool row_in = gy >= 0 && gy < dy;
-    for (int lx = lane; lx < tx + 2 * R; lx += 32) {
-      const int gx = x0 - R + lx;
-      sm.occ[ly][lx] = (row_in && gx >= 0 && gx < dx) ? src[(int64_t)gy * dx + gx] : 0;
-    }
+  static_assert(R >= 1 && R <= PB_HALO - 2, "radius must leave the 28-bit window inside the staged halo");
+  constexpr int ROWS = PB_TY + 2 * R, WPR = (PB_TX + 2 * PB_HALO) / 4, GPR = PB_TX / 4;
+  const int64_t X = occ_pitch(dx);
+  const int64_t zbase = (int64_t)z * dy * X;
+  for (int i = threadIdx.x; i < ROWS * WPR; i += blockDim.x) {
+    const int ly = i / WPR, w = i - ly * WPR;
+    const int gy = y0 - R + ly, gx = x0 - PB_HALO + 4 * w;
+    uint32_t v = 0;
+    if (gy >= 0 && gy < dy && gx >= 0 && gx < X)
+      v = *reinterpret_cast<const uint32_t*>(occ + zbase + (int64_t)gy * X + gx);
+    sm.occ[ly][w] = v;
   }
   __syncthreads();
-  for (int ly = warp; ly < PA_TY + 2 * R; ly += 8)
-    for (int lx = lane; lx < tx; lx += 32) {
-      int best = kNone8;
+  const int ngr = (min(PB_TX, dx - x0) + 3) / 4;
+  for (int i = threadIdx.x; i < ROWS * GPR; i += blockDim.x) {
+    const int ly = i / GPR, g = i - ly * GPR;
+    if (g >= ngr) continue;
+    uint32_t mask = 0;  // bit k <-> staged byte 4g + k
 #pragma unroll
-      for (int d = -R; d <= R; ++d)
-        if (sm.occ[ly][lx + R + d]) best = min(best, d * d);
-      sm.g1[ly][lx] = (uint8_t)best;
+    for (int k = 0; k < 7; ++k) {
+      const uint32_t w = sm.occ[ly][g + k] & 0x01010101u;
+      mask |= ((w | (w >> 7) | (w >> 14) | (w >> 21)) & 0xFu) << (4 * k);
     }
-  __syncthreads();
-  const int ny = min(PA_TY, dy - y0);
-  uint8_t* dst = g2 + (int64_t)z * plane;
-  for (int ly = warp; ly < ny; ly += 8)
-    for (int lx = lane; lx < tx; lx += 32) {
-      int best = kNone8;
+    uint32_t out = 0;
 #pragma unroll
-      for (int d = -R; d <= R; ++d) {
-        int v = sm.g1[ly + R + d][lx];
-        if (v != kNone8) best = min(best, v + d * d);
+    for (int q = 0; q < 4; ++q) {
+      const int c = PB_HALO + q;  // bit of position x0 + 4g + q
+      int best = kNone8;
+      const uint32_t rw = (mask >> c) & ((1u << (R + 1)) - 1);  // offsets 0..R
+      if (rw) {
+        const int d = __ffs(rw) - 1;
+        best = d * d;
       }
-      dst[(int64_t)(y0 + ly) * dx + x0 + lx] = (uint8_t)best;
+      const uint32_t lw = (mask >> (c - R)) & ((1u << R) - 1);  // offsets -R..-1
+      if (lw) {
+        const int d = R - (31 - __clz(lw));
+        best = min(best, d * d);
+      }
+      out |= (uint32_t)best << (8 * q);
     }
+    sm.g1[ly][g] = out;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < PB_TY * GPR; i += blockDim.x) {
+    const int ly = i / GPR, g = i - ly * GPR;
+    if (y0 + ly >= dy || g >= ngr) continue;
+    uint32_t best = 0xFFFFFFFFu;
+#pragma unroll
+    for (int d = -R; d <= R; ++d) best = __vminu4(best, __vaddus4(sm.g1[ly + R + d][g], (uint32_t)(d * d) * 0x01010101u));
+    *reinterpret_cast<uint32_t*>(g2 + zbase + (int64_t)(y0 + ly) * X + x0 + 4 * g) = best;
+  }
 }
 
-// Pass along z for voxel v (z = v / plane), then the TDF value.  Distance 0
-// is the voxel's own occupancy, so 1 - sqrtf(0)/R = 1 reproduces the
-// reference's "occupied -> 1" (core/demo.cu:40-43).
+// TDF value of a saturated squared distance: max(0, 1 - sqrtf(g)/R), the
+// reference's expression (core/demo.cu:44-56) in IEEE operations; g >= R^2
+// gives 0, so the 0xFF saturation is exact.  Filled by the calling block.
 template <int R>
-__device__ __forceinline__ float z_voxel(const uint8_t* __restrict__ g2, int64_t plane, int dz, int64_t v) {
-  const int z = (int)(v / plane);
-  int best = 0xFFFF;
-#pragma unroll
-  for (int d = -R; d <= R; ++d) {
-    const int zz = z + d;
-    if (zz < 0 || zz >= dz) continue;
-    const int g = __ldg(g2 + v + (int64_t)d * plane);
-    if (g != kNone8) best = min(best, g + d * d);
+__device__ __forceinline__ void tdf_lut(float* lut) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    const float v = __fsub_rn(1.0f, __fdiv_rn(__fsqrt_rn((float)i), (float)R));
+    lut[i] = v > 0.0f ? v : 0.0f;
   }
-  if (best == 0xFFFF) return 0.0f;
-  const float val = __fsub_rn(1.0f, __fdiv_rn(__fsqrt_rn((float)best), (float)R));
-  return val > 0.0f ? val : 0.0f;
+}
+
+// Pass along z by one warp over a column segment: lane l owns the 4 voxels
+// x = xseg + 4l .. +3 of row y and walks z = z0 .. z1-1 with the 2R+1 words
+// of g2 around z in a register ring (one new aligned load per step).  Values
+// go through the warp's 128-float staging area so each store instruction
+// writes 32 consecutive floats.  Must be called by all 32 lanes.
+constexpr int kZChunk = 32;  // z steps per warp work item
+template <int R>
+__device__ __forceinline__ void z_column(const uint8_t* __restrict__ g2, int dx, int dy, int dz, int y, int xseg,
+                                         int z0, int z1, const float* lut, float* s_w, float* __restrict__ tdf) {
+  const int lane = threadIdx.x & 31;
+  const int64_t X = occ_pitch(dx), pz = (int64_t)dy * X;
+  const int x4 = xseg + 4 * lane;
+  const bool live = x4 < dx;
+  const uint8_t* col = g2 + (int64_t)y * X + x4;
+  auto word = [&](int zz) -> uint32_t {
+    return (live && zz >= 0 && zz < dz) ? __ldg(reinterpret_cast<const uint32_t*>(col + zz * pz)) : 0xFFFFFFFFu;
+  };
+  uint32_t ring[2 * R + 1];
+#pragma unroll
+  for (int k = 0; k < 2 * R + 1; ++k) ring[k] = word(z0 - R + k);
+  const int n = min(128, dx - xseg);
+  for (int z = z0; z < z1; ++z) {
+    uint32_t best = 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < 2 * R + 1; ++k)
+      best = __vminu4(best, __vaddus4(ring[k], (uint32_t)((k - R) * (k - R)) * 0x01010101u));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s_w[4 * lane + q] = lut[(best >> (8 * q)) & 0xFFu];
+    __syncwarp();
+    float* out = tdf + ((int64_t)z * dy + y) * dx + xseg;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (lane + 32 * i < n) out[lane + 32 * i] = s_w[lane + 32 * i];
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 2 * R; ++k) ring[k] = ring[k + 1];
+    ring[2 * R] = word(z + R + 1);
+  }
 }
 
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {

@@ -77,8 +77,8 @@ tdm_status tdm_grid_from_points(const float* pts_dev, int32_t n, float voxel_siz
                                 tdm_grid* grid_out, void* ws_dev, tdm_stream s);
 /* TDF of core/demo.cu:22-57 over the whole grid: occupancy scatter of the
  * points, exact windowed squared distance, 1 - d/trunc.  tdf_dev: V floats.
- * ws_dev: tdm_tdf_workspace_bytes(grid) = 2 V bytes (occupancy, then the
- * in-plane squared distances). */
+ * ws_dev: tdm_tdf_workspace_bytes(grid) bytes: occupancy, then the in-plane
+ * squared distances, one byte per voxel each with x rows padded to 4. */
 size_t tdm_tdf_workspace_bytes(const tdm_grid* grid);
 tdm_status tdm_tdf(const float* pts_dev, int32_t n, const tdm_grid* grid, int32_t decode_mode, float* tdf_dev,
                    void* ws_dev, size_t ws_bytes, tdm_stream s);
@@ -269,7 +269,8 @@ typedef struct tdm_batch_config {
   int32_t max_fragments; /* <= 1024 */
   int64_t max_points;    /* over the batch */
   int64_t max_keypoints; /* over the batch */
-  int64_t max_voxels;    /* over the batch (each grid rounded up to 256) */
+  int64_t max_voxels;    /* over the batch (each grid with its x rows padded to a
+                          * multiple of 4, then rounded up to 256) */
   float trunc_voxels;    /* truncation in voxels (5) for every fragment */
   int32_t pad;           /* 15 */
   int32_t use_graph;
