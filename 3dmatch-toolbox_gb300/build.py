@@ -4,6 +4,7 @@ Compiles every translation unit in parallel with nvcc / g++ and links in-tree:
     lib/libtdm.so      the C ABI of include/tdm.h
     bin/demo           drop-in for core/demo.cu's `demo <cloud.ply> <out_prefix>`
     bin/fuse           drop-in for depth-fusion/demo.cu
+    bin/descriptors    drop-in for evaluation/*/get3DMatchDescriptors.cu
 Objects go to _build/.  Rebuilds only what changed (sources or headers).
 """
 from __future__ import annotations
@@ -109,12 +110,17 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         tmp = LIB_PATH + ".tmp%d" % os.getpid()
         _run([_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
         os.replace(tmp, LIB_PATH)
-    for tool in ("demo", "fuse"):
+    # the command-line drop-ins; a tool that cannot be built (fuse needs zlib)
+    # is reported and left out, the library stands on its own
+    for tool, libs in (("demo", []), ("fuse", ["-lz"]), ("descriptors", [])):
         src = os.path.join(HOST, tool + ".cpp")
         out = os.path.join(BIN, tool)
         if os.path.exists(src) and _stale(out, [src, LIB_PATH] + hdrs):
-            _run(["g++"] + CXX_FLAGS + [src, "-o", out, "-L" + LIB, "-ltdm", "-Wl,-rpath,$ORIGIN/../lib",
-                                       "-L/usr/local/cuda/lib64", "-lcudart"])
+            try:
+                _run(["g++"] + CXX_FLAGS + [src, "-o", out, "-L" + LIB, "-ltdm", "-Wl,-rpath,$ORIGIN/../lib",
+                                           "-L/usr/local/cuda/lib64", "-lcudart"] + libs)
+            except RuntimeError as e:
+                print("warning: bin/%s not built: %s" % (tool, str(e).splitlines()[-1][:300]))
     if verbose:
         print("built", LIB_PATH)
     return LIB_PATH
