@@ -42,6 +42,7 @@ EXPORTS = [
     "tdm_server_create", "tdm_server_slots", "tdm_server_submit", "tdm_server_wait", "tdm_server_destroy",
     "tdm_net_autotune", "tdm_net_tiles", "tdm_net_set_tile",
     "tdm_batch_create", "tdm_batch_destroy", "tdm_batch_device_bytes", "tdm_describe_batch", "tdm_batch_stats",
+    "tdm_overlap_workspace_bytes", "tdm_overlap",
 ]
 
 
@@ -159,6 +160,8 @@ def lib():
         "tdm_batch_device_bytes": (sz, [P]),
         "tdm_describe_batch": (i32, [P, P, i32, P, P, P, P, P, P, P, P]),
         "tdm_batch_stats": (i32, [P, P, P]),
+        "tdm_overlap_workspace_bytes": (sz, [i32, i32]),
+        "tdm_overlap": (i32, [P, i32, P, i32, P, f32, P, P, sz, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name, None)
@@ -390,6 +393,21 @@ def ransac(x_dev, y_dev, m_dev, seed: int, iterations: int, threshold=0.05, adap
     check(lib().tdm_ransac(_ptr(x_dev), _ptr(y_dev), _ptr(m_dev), m_max, ctypes.byref(prm), _ptr(rt), _ptr(inl),
                            _ptr(info), _ptr(ws), nws, _stream(stream)))
     return rt, inl, info
+
+
+def overlap(a_dev, b_dev, rt, radius=0.05, stream=None):
+    """(points of a near Rt*b, points of Rt*b near a) within radius: the
+    reference's ratioAligned numerators (register2Fragments.m:90-97)."""
+    import torch
+    na, nb = a_dev.shape[0], b_dev.shape[0]
+    r = np.ascontiguousarray(np.asarray(rt, np.float64).reshape(-1)[:12])
+    counts = torch.zeros(2, dtype=torch.int32, device=a_dev.device)
+    nws = lib().tdm_overlap_workspace_bytes(na, nb)
+    ws = torch.empty(max(nws, 16), dtype=torch.uint8, device=a_dev.device)
+    check(lib().tdm_overlap(_ptr(a_dev), na, _ptr(b_dev), nb, _ptr(r), radius, _ptr(counts), _ptr(ws), nws,
+                            _stream(stream)))
+    c = counts.cpu().numpy()
+    return int(c[0]), int(c[1])
 
 
 def pairs_to_points(kp_a, kp_b, pairs, n_pairs_dev, stream=None):

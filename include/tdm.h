@@ -200,6 +200,19 @@ tdm_status tdm_pairs_to_points(const float* kp_a_dev, const float* kp_b_dev, con
                                const int32_t* n_pairs_dev, int32_t max_pairs, float* x_dev, float* y_dev,
                                tdm_stream s);
 
+/* ---- surface overlap of a registered pair: replaces the 1-NN overlap of
+ * core/demo.m:66-72 and evaluation/geometric-registration/register2Fragments.m:90-97
+ * (multiQueryKNNSearchImpl + sum(dists < 0.05)) ------------------------------ */
+/* counts_dev[0] = points of a with a point of Rt*b closer than radius,
+ * counts_dev[1] = points of Rt*b with a point of a closer than radius
+ * (ratioAligned = counts / sizes).  rt_host: row-major 3x4 double (x_a = R x_b
+ * + t), applied in float.  Clouds of 1 .. 524288 points whose coordinates stay
+ * within 65536 * 1.05 * radius of the origin (3.4 km at 5 cm).  Exact float
+ * distances (d2 < r*r); synchronizes the stream. */
+size_t tdm_overlap_workspace_bytes(int32_t na, int32_t nb);
+tdm_status tdm_overlap(const float* a_dev, int32_t na, const float* b_dev, int32_t nb, const double rt_host[12],
+                       float radius, int32_t* counts_dev, void* ws_dev, size_t ws_bytes, tdm_stream s);
+
 /* ---- TSDF fusion: replaces depth-fusion/demo.cu:18-68 (Integrate) and
  * core/utils.hpp:23-65 (SaveVoxelGrid2SurfacePointCloud) -------------------- */
 /* tsdf = 1, weight = 0 (depth-fusion/demo.cu:131-135). */

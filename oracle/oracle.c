@@ -647,3 +647,45 @@ int64_t orc_extract_surface(const float* tsdf, const float* weight, const int di
   }
   return n;
 }
+
+/* Surface overlap (core/demo.m:66-72, register2Fragments.m:90-97): counts[0]
+ * = points of a with a point of Rt*b closer than radius, counts[1] = points
+ * of Rt*b with a point of a closer than radius, by brute force.  b is moved
+ * in float with R, t rounded from double: ((R0 x + R1 y) + R2 z) + t;
+ * d2 = (dx dx + dy dy) + dz dz < radius * radius in float. */
+void orc_overlap(const float* a, int na, const float* b, int nb, const double rt[12], float radius, int32_t counts[2]) {
+  float R[9] = {(float)rt[0], (float)rt[1], (float)rt[2], (float)rt[4], (float)rt[5],
+                (float)rt[6], (float)rt[8], (float)rt[9], (float)rt[10]};
+  float t[3] = {(float)rt[3], (float)rt[7], (float)rt[11]};
+  float* bt = (float*)malloc(sizeof(float) * 3 * (size_t)nb);
+  for (int i = 0; i < nb; ++i)
+    for (int r = 0; r < 3; ++r) {
+      float v = R[3 * r] * b[3 * i];
+      v = v + R[3 * r + 1] * b[3 * i + 1];
+      v = v + R[3 * r + 2] * b[3 * i + 2];
+      bt[3 * i + r] = v + t[r];
+    }
+  const float r2 = radius * radius;
+  const float* q[2] = {a, bt};
+  const float* ref[2] = {bt, a};
+  const int nq[2] = {na, nb}, nr[2] = {nb, na};
+  for (int dir = 0; dir < 2; ++dir) {
+    int32_t cnt = 0;
+#pragma omp parallel for reduction(+ : cnt) schedule(dynamic, 256)
+    for (int i = 0; i < nq[dir]; ++i) {
+      const float* p = q[dir] + 3 * (size_t)i;
+      for (int j = 0; j < nr[dir]; ++j) {
+        const float* s = ref[dir] + 3 * (size_t)j;
+        float dx = p[0] - s[0], dy = p[1] - s[1], dz = p[2] - s[2];
+        float d2 = dx * dx + dy * dy;
+        d2 = d2 + dz * dz;
+        if (d2 < r2) {
+          ++cnt;
+          break;
+        }
+      }
+    }
+    counts[dir] = cnt;
+  }
+  free(bt);
+}

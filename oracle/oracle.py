@@ -85,6 +85,7 @@ def lib():
             "orc_tsdf_integrate": (None, [P, P, P, i32, i32, P, P, f32, f32, P, P]),
             "orc_tsdf_integrate_z": (None, [P, P, P, i32, i32, P, P, f32, f32, i32, i32, P, P]),
             "orc_extract_surface": (i64, [P, P, P, P, f32, f32, f32, P]),
+            "orc_overlap": (None, [P, i32, P, i32, P, f32, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -289,6 +290,16 @@ def net_forward(patches: np.ndarray, weights: dict, use_feat: bool = True, f64: 
 # --------------------------------------------------------------------------
 # Matching and registration
 # --------------------------------------------------------------------------
+def overlap(a: np.ndarray, b: np.ndarray, rt, radius=0.05):
+    """(points of a near Rt*b, points of Rt*b near a): register2Fragments.m:90-97."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    r = np.ascontiguousarray(np.asarray(rt, np.float64).reshape(-1)[:12])
+    c = np.zeros(2, np.int32)
+    lib().orc_overlap(_p(a), a.shape[0], _p(b), b.shape[0], _p(r), radius, _p(c))
+    return int(c[0]), int(c[1])
+
+
 def mutual_nn(da: np.ndarray, db: np.ndarray):
     da = np.ascontiguousarray(da, np.float32)
     db = np.ascontiguousarray(db, np.float32)
