@@ -46,6 +46,27 @@ def write_log(path, records):
                 f.write("%.10f\t%.10f\t%.10f\t%.10f\n" % tuple(row))
 
 
+def write_info(path, records):
+    """getGtInfoLog.m's gt.info layout: "%d\t %d\t %d\t" then six rows of "%15.8e"."""
+    with open(path, "w") as f:
+        for i, j, n, m in records:
+            f.write("%d\t %d\t %d\t\n" % (i, j, n))
+            for row in np.asarray(m, np.float64).reshape(6, 6):
+                f.write("\t ".join("%15.8e" % v for v in row) + "\t\n")
+
+
+def gt_information(corres_points):
+    """getGtInfoLog.m: sum over ground-truth correspondence points q of G^T G,
+    G = [I, -[q]x]."""
+    q = np.asarray(corres_points, np.float64).reshape(-1, 3)
+    M = np.zeros((6, 6))
+    for x, y, z in q:
+        Qx = np.array([[0.0, -z, y], [z, 0.0, -x], [-y, x, 0.0]])
+        G = np.concatenate([np.eye(3), -Qx], 1)
+        M += G.T @ G
+    return M
+
+
 def log_records(results, n_fragments, min_overlap=0.30):
     """Pairs to log (writeLog.m): results are (i, j, rt 4x4, overlap on the
     first fragment); kept when the overlap is above min_overlap."""
@@ -64,7 +85,6 @@ def evaluate_registration(result, gt, gt_info, err2=0.04):
     """(recall, precision) of mrEvaluateRegistration.m over non-consecutive pairs."""
     if not gt:
         return 0.0, 0.0
-    n = gt[0][2]
     index = {(i, j): k for k, (i, j, _, _) in enumerate(gt) if j - i > 1}
     info = {(i, j): m for i, j, _, m in gt_info}
     logged = good = 0

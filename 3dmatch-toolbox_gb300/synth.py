@@ -132,6 +132,27 @@ def fragment_pair(seed: int, n_points=150_000, max_deg=30.0, max_t=0.5):
     return out[0], out[1], Rt
 
 
+def scene_fragments(seed: int, n_views=8, n_points=150_000):
+    """Fragments of one room seen from cameras along a sweep (x from 1 to 3 m,
+    looking towards the far wall with a slowly turning yaw).  Returns
+    [(points float32 in the camera frame, camera-to-world 4x4)]; the
+    ground-truth transform of fragment j into fragment i's frame is
+    inv(cam_i) @ cam_j (getGtInfoLog.m's relExt)."""
+    rng = np.random.default_rng(seed)
+    room = Room(seed)
+    out = []
+    for v in range(n_views):
+        s = v / max(n_views - 1, 1)
+        eye = np.array([1.0 + 2.0 * s, rng.uniform(0.4, 0.7), rng.uniform(1.3, 1.6)])
+        target = np.array([1.0 + 2.0 * s + 1.2 * np.sin(2.5 * s - 1.2), 4.0, rng.uniform(0.7, 1.2)])
+        cam = look_at(eye, target)
+        p = backproject(render_depth(room, cam, rng))
+        if n_points is not None and p.shape[0] > n_points:
+            p = p[np.sort(rng.choice(p.shape[0], n_points, replace=False))]
+        out.append((p.astype(np.float32), cam))
+    return out
+
+
 def fragment(seed: int, n_points=150_000):
     return fragment_pair(seed, n_points)[0]
 

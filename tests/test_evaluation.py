@@ -65,3 +65,18 @@ def test_fpr_definition(ev):
     d = np.concatenate([np.linspace(0.0, 1.0, 100), np.linspace(2.0, 3.0, 100)])
     m = np.concatenate([np.ones(100), np.zeros(100)])
     assert ev.fpr_at_95_recall(d, m) == 0.0
+
+
+def test_info_roundtrip_and_information(ev, tmp_path):
+    q = np.random.default_rng(3).normal(size=(50, 3))
+    M = ev.gt_information(q)
+    assert np.allclose(M, M.T) and np.allclose(M[:3, :3], 50 * np.eye(3))
+    ev.write_info(tmp_path / "g.info", [(0, 2, 5, M)])
+    (i, j, n, back), = ev.read_info(tmp_path / "g.info")
+    assert (i, j, n) == (0, 2, 5) and np.allclose(back, M, rtol=1e-7)
+    # a result equal to the ground truth is correct; one 0.5 m off is not
+    gt = [(0, 2, 5, np.eye(4))]
+    off = np.eye(4)
+    off[0, 3] = 0.5
+    assert ev.evaluate_registration([(0, 2, 5, np.eye(4))], gt, [(0, 2, 5, M)]) == (1.0, 1.0)
+    assert ev.evaluate_registration([(0, 2, 5, off)], gt, [(0, 2, 5, M)]) == (0.0, 0.0)
