@@ -42,7 +42,7 @@ EXPORTS = [
     "tdm_server_create", "tdm_server_slots", "tdm_server_submit", "tdm_server_wait", "tdm_server_destroy",
     "tdm_net_autotune", "tdm_net_tiles", "tdm_net_set_tile",
     "tdm_batch_create", "tdm_batch_destroy", "tdm_batch_device_bytes", "tdm_describe_batch", "tdm_batch_stats",
-    "tdm_overlap_workspace_bytes", "tdm_overlap",
+    "tdm_overlap_workspace_bytes", "tdm_overlap", "tdm_tdf_exact",
 ]
 
 
@@ -162,6 +162,7 @@ def lib():
         "tdm_batch_stats": (i32, [P, P, P]),
         "tdm_overlap_workspace_bytes": (sz, [i32, i32]),
         "tdm_overlap": (i32, [P, i32, P, i32, P, f32, P, P, sz, P]),
+        "tdm_tdf_exact": (i32, [P, i32, G, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name, None)
@@ -393,6 +394,14 @@ def ransac(x_dev, y_dev, m_dev, seed: int, iterations: int, threshold=0.05, adap
     check(lib().tdm_ransac(_ptr(x_dev), _ptr(y_dev), _ptr(m_dev), m_max, ctypes.byref(prm), _ptr(rt), _ptr(inl),
                            _ptr(info), _ptr(ws), nws, _stream(stream)))
     return rt, inl, info
+
+
+def tdf_exact(pts_dev, grid: Grid, stream=None):
+    """pointCloud2TDF.m on the grid's voxel centres (float [V], x fastest)."""
+    import torch
+    out = torch.empty(grid.voxels, dtype=torch.float32, device=pts_dev.device)
+    check(lib().tdm_tdf_exact(_ptr(pts_dev), pts_dev.shape[0], ctypes.byref(grid), _ptr(out), _stream(stream)))
+    return out
 
 
 def overlap(a_dev, b_dev, rt, radius=0.05, stream=None):

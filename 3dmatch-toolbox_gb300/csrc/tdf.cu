@@ -186,6 +186,58 @@ __global__ __launch_bounds__(256) void gather_kernel(const float* __restrict__ t
                patches + (int64_t)k * 27000);
 }
 
+// Exact TDF (evaluation/model-fitting-apc/pointCloud2TDF.m,
+// deprecated/pointCloud2AccTDF.m): 1 - min(d / trunc, 1) with d the distance
+// from the voxel centre o + i vs to the nearest point.  Each point lowers the
+// squared distance of every voxel centre within trunc (atomicMin on the bits
+// of a non-negative float orders like the float); untouched voxels keep +inf
+// and become 0.
+__global__ void exact_fill_kernel(uint32_t* __restrict__ d2, int64_t V) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < V; i += (int64_t)gridDim.x * blockDim.x)
+    d2[i] = 0x7F800000u;
+}
+
+__global__ void exact_scatter_kernel(const float* __restrict__ pts, int n, int dx, int dy, int dz, float ox, float oy,
+                                     float oz, float vs, float trunc, uint32_t* __restrict__ d2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float p[3] = {pts[3 * (int64_t)i], pts[3 * (int64_t)i + 1], pts[3 * (int64_t)i + 2]};
+  const float o[3] = {ox, oy, oz};
+  const int dim[3] = {dx, dy, dz};
+  int lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) {
+    const float u = (p[a] - o[a]) / vs, w = trunc / vs;
+    if (!(u - w < 2.0e9f && u + w > -2.0e9f)) return;  // non-finite or absurd coordinates touch no voxel
+    lo[a] = max(0, (int)ceilf(u - w) - 1);
+    hi[a] = min(dim[a] - 1, (int)floorf(u + w) + 1);
+    if (lo[a] > hi[a]) return;
+  }
+  // centre - point in double: a float centre o + i vs carries ~1e-7 of the
+  // coordinate's magnitude, which is more than the 1e-6 TDF budget allows
+  const double t2 = (double)trunc * trunc, vsd = vs;
+  for (int z = lo[2]; z <= hi[2]; ++z) {
+    const double ez = ((double)o[2] + z * vsd) - p[2];
+    for (int y = lo[1]; y <= hi[1]; ++y) {
+      const double ey = ((double)o[1] + y * vsd) - p[1];
+      const double eyz = ey * ey + ez * ez;
+      if (eyz >= t2) continue;
+      for (int x = lo[0]; x <= hi[0]; ++x) {
+        const double ex = ((double)o[0] + x * vsd) - p[0];
+        const double e2 = ex * ex + eyz;
+        if (e2 < t2) atomicMin(d2 + ((int64_t)z * dy + y) * dx + x, __float_as_uint((float)e2));
+      }
+    }
+  }
+}
+
+__global__ void exact_value_kernel(float* __restrict__ tdf, int64_t V, float trunc) {
+  uint32_t* d2 = reinterpret_cast<uint32_t*>(tdf);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < V; i += (int64_t)gridDim.x * blockDim.x) {
+    const float e2 = __uint_as_float(d2[i]);
+    tdf[i] = 1.0f - fminf(sqrtf(e2) / trunc, 1.0f);
+  }
+}
+
 template <int R>
 void launch_tdf(const uint8_t* occ, uint8_t* g2, const tdm_grid* g, float* tdf, cudaStream_t s) {
   dim3 ga((g->dim[0] + PB_TX - 1) / PB_TX, (g->dim[1] + PB_TY - 1) / PB_TY, g->dim[2]);
@@ -267,6 +319,22 @@ extern "C" tdm_status tdm_tdf(const float* pts, int32_t n, const tdm_grid* g, in
                                                                         mode, first_bad, (int64_t)V, tdf);
     TDM_CHECK_LAUNCH("tdf_refcompat_kernel");
   }
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_tdf_exact(const float* pts, int32_t n, const tdm_grid* g, float* tdf, tdm_stream s) {
+  TDM_REQUIRE(pts && g && tdf && n > 0, "tdm_tdf_exact: null pointer or n <= 0");
+  TDM_REQUIRE(g->voxel_size > 0.0f && g->trunc_margin > 0.0f, "tdm_tdf_exact: voxel size and truncation must be > 0");
+  TDM_REQUIRE(g->trunc_margin <= 32.0f * g->voxel_size, "tdm_tdf_exact: truncation above 32 voxels");
+  const int64_t V = (int64_t)g->dim[0] * g->dim[1] * g->dim[2];
+  TDM_REQUIRE(V > 0, "tdm_tdf_exact: empty grid");
+  uint32_t* d2 = reinterpret_cast<uint32_t*>(tdf);
+  exact_fill_kernel<<<(unsigned)std::min<int64_t>((V + 255) / 256, 8192), 256, 0, s>>>(d2, V);
+  exact_scatter_kernel<<<(n + 127) / 128, 128, 0, s>>>(pts, n, g->dim[0], g->dim[1], g->dim[2], g->origin[0],
+                                                       g->origin[1], g->origin[2], g->voxel_size, g->trunc_margin, d2);
+  exact_value_kernel<<<(unsigned)std::min<int64_t>((V + 255) / 256, 8192), 256, 0, s>>>(tdf, V, g->trunc_margin);
+  note_launches(2);
+  TDM_CHECK_LAUNCH("tdm_tdf_exact");
   return TDM_OK;
 }
 

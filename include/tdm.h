@@ -80,6 +80,12 @@ tdm_status tdm_grid_from_points(const float* pts_dev, int32_t n, float voxel_siz
  * ws_dev: tdm_tdf_workspace_bytes(grid) bytes: occupancy, then the in-plane
  * squared distances, one byte per voxel each with x rows padded to 4. */
 size_t tdm_tdf_workspace_bytes(const tdm_grid* grid);
+/* Exact TDF of evaluation/model-fitting-apc/pointCloud2TDF.m (and
+ * deprecated/pointCloud2AccTDF.m): 1 - min(d / trunc_margin, 1) with d the
+ * distance from the voxel centre origin + i * voxel_size to the nearest point
+ * (float arithmetic; within 1e-6 of the double-precision distance).  No
+ * workspace; trunc_margin <= 32 voxels. */
+tdm_status tdm_tdf_exact(const float* pts_dev, int32_t n, const tdm_grid* grid, float* tdf_dev, tdm_stream s);
 tdm_status tdm_tdf(const float* pts_dev, int32_t n, const tdm_grid* grid, int32_t decode_mode, float* tdf_dev,
                    void* ws_dev, size_t ws_bytes, tdm_stream s);
 

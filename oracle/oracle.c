@@ -689,3 +689,26 @@ void orc_overlap(const float* a, int na, const float* b, int nb, const double rt
   }
   free(bt);
 }
+
+/* Exact TDF (evaluation/model-fitting-apc/pointCloud2TDF.m): for every voxel
+ * centre c = o + i vs (double), d = distance to the nearest point (double,
+ * brute force over the points), tdf = 1 - min(d / trunc, 1). */
+void orc_tdf_exact(const float* pts, int n, const int dim[3], const float origin[3], float vs, float trunc, float* tdf) {
+  const int64_t V = (int64_t)dim[0] * dim[1] * dim[2];
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t v = 0; v < V; ++v) {
+    const int64_t z = v / ((int64_t)dim[0] * dim[1]);
+    const int64_t y = (v / dim[0]) % dim[1];
+    const int64_t x = v % dim[0];
+    const double c[3] = {(double)origin[0] + x * (double)vs, (double)origin[1] + y * (double)vs,
+                         (double)origin[2] + z * (double)vs};
+    double best = INFINITY;
+    for (int i = 0; i < n; ++i) {
+      const double ex = c[0] - pts[3 * i], ey = c[1] - pts[3 * i + 1], ez = c[2] - pts[3 * i + 2];
+      const double d2 = ex * ex + ey * ey + ez * ez;
+      if (d2 < best) best = d2;
+    }
+    const double t = sqrt(best) / trunc;
+    tdf[v] = (float)(1.0 - (t < 1.0 ? t : 1.0));
+  }
+}

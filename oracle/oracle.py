@@ -86,6 +86,7 @@ def lib():
             "orc_tsdf_integrate_z": (None, [P, P, P, i32, i32, P, P, f32, f32, i32, i32, P, P]),
             "orc_extract_surface": (i64, [P, P, P, P, f32, f32, f32, P]),
             "orc_overlap": (None, [P, i32, P, i32, P, f32, P]),
+            "orc_tdf_exact": (None, [P, i32, P, P, f32, f32, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -290,6 +291,16 @@ def net_forward(patches: np.ndarray, weights: dict, use_feat: bool = True, f64: 
 # --------------------------------------------------------------------------
 # Matching and registration
 # --------------------------------------------------------------------------
+def tdf_exact(pts: np.ndarray, dim, origin, vs, trunc):
+    """pointCloud2TDF.m restated (double distances), x fastest."""
+    pts = np.ascontiguousarray(pts, np.float32)
+    d = np.ascontiguousarray(dim, np.int32)
+    o = np.ascontiguousarray(origin, np.float32)
+    out = np.zeros(int(d[0]) * int(d[1]) * int(d[2]), np.float32)
+    lib().orc_tdf_exact(_p(pts), pts.shape[0], _p(d), _p(o), vs, trunc, _p(out))
+    return out
+
+
 def overlap(a: np.ndarray, b: np.ndarray, rt, radius=0.05):
     """(points of a near Rt*b, points of Rt*b near a): register2Fragments.m:90-97."""
     a = np.ascontiguousarray(a, np.float32)

@@ -106,3 +106,16 @@ def test_gather_edges_read_zero(tdm, oracle, cuda, small):
     got = tdm.gather(tdf, g, torch.from_numpy(kg).to(cuda)).cpu().numpy()
     want = oracle.gather(tdf.cpu().numpy(), dim, kg)
     assert np.array_equal(got, want)
+
+
+def test_tdf_exact_against_oracle(tdm, oracle, cuda, scene):
+    """pointCloud2TDF.m: nearest-point distance from every voxel centre,
+    within 1e-6 of the oracle's double-precision values."""
+    import torch
+    pts = scene.fragment(20267000, n_points=3000)
+    pts = pts[(pts[:, 2] < 2.0)][:2000]
+    g = tdm.grid_from_points_host(pts, voxel_size=0.02, trunc_voxels=5.0, pad=3)
+    got = tdm.tdf_exact(torch.from_numpy(np.ascontiguousarray(pts)).to(cuda), g).cpu().numpy()
+    want = oracle.tdf_exact(pts, list(g.dim), list(g.origin), g.voxel_size, g.trunc_margin)
+    assert np.abs(got - want).max() <= 1e-6
+    assert (want > 0).sum() > 1000  # the surface band is covered
