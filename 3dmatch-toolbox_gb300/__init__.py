@@ -42,7 +42,7 @@ EXPORTS = [
     "tdm_server_create", "tdm_server_slots", "tdm_server_submit", "tdm_server_wait", "tdm_server_destroy",
     "tdm_net_autotune", "tdm_net_tiles", "tdm_net_set_tile",
     "tdm_batch_create", "tdm_batch_destroy", "tdm_batch_device_bytes", "tdm_describe_batch", "tdm_batch_stats",
-    "tdm_overlap_workspace_bytes", "tdm_overlap", "tdm_tdf_exact",
+    "tdm_overlap_workspace_bytes", "tdm_overlap", "tdm_tdf_exact", "tdm_icp_workspace_bytes", "tdm_icp",
 ]
 
 
@@ -79,6 +79,17 @@ class BatchConfig(ctypes.Structure):
     _fields_ = [("max_fragments", ctypes.c_int32), ("max_points", ctypes.c_int64), ("max_keypoints", ctypes.c_int64),
                 ("max_voxels", ctypes.c_int64), ("trunc_voxels", ctypes.c_float), ("pad", ctypes.c_int32),
                 ("use_graph", ctypes.c_int32)]
+
+
+class IcpParams(ctypes.Structure):
+    _fields_ = [("grid", ctypes.c_float), ("max_dist", ctypes.c_float), ("inlier_ratio", ctypes.c_float),
+                ("max_iterations", ctypes.c_int32), ("tol_translation", ctypes.c_float),
+                ("tol_rotation_deg", ctypes.c_float)]
+
+
+class IcpResult(ctypes.Structure):
+    _fields_ = [("rt", ctypes.c_double * 12), ("iterations", ctypes.c_int32), ("correspondences", ctypes.c_int32),
+                ("rmse", ctypes.c_float), ("converged", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -163,6 +174,8 @@ def lib():
         "tdm_overlap_workspace_bytes": (sz, [i32, i32]),
         "tdm_overlap": (i32, [P, i32, P, i32, P, f32, P, P, sz, P]),
         "tdm_tdf_exact": (i32, [P, i32, G, P, P]),
+        "tdm_icp_workspace_bytes": (sz, [i32, i32]),
+        "tdm_icp": (i32, [P, i32, P, i32, P, ctypes.POINTER(IcpParams), ctypes.POINTER(IcpResult), P, sz, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name, None)
@@ -402,6 +415,24 @@ def tdf_exact(pts_dev, grid: Grid, stream=None):
     out = torch.empty(grid.voxels, dtype=torch.float32, device=pts_dev.device)
     check(lib().tdm_tdf_exact(_ptr(pts_dev), pts_dev.shape[0], ctypes.byref(grid), _ptr(out), _stream(stream)))
     return out
+
+
+def icp(fixed_dev, moving_dev, init_rt, grid=0.01, max_dist=0.10, inlier_ratio=0.30, max_iterations=50,
+        tol_translation=1e-4, tol_rotation_deg=9e-5, stream=None):
+    """ICP of moving onto fixed from init_rt (3x4 or 4x4, moving -> fixed):
+    (4x4 float64, IcpResult)."""
+    import torch
+    nf, nm = fixed_dev.shape[0], moving_dev.shape[0]
+    r = np.ascontiguousarray(np.asarray(init_rt, np.float64).reshape(-1)[:12])
+    prm = IcpParams(grid, max_dist, inlier_ratio, max_iterations, tol_translation, tol_rotation_deg)
+    res = IcpResult()
+    nws = lib().tdm_icp_workspace_bytes(nf, nm)
+    ws = torch.empty(max(nws, 16), dtype=torch.uint8, device=fixed_dev.device)
+    check(lib().tdm_icp(_ptr(fixed_dev), nf, _ptr(moving_dev), nm, _ptr(r), ctypes.byref(prm), ctypes.byref(res),
+                        _ptr(ws), nws, _stream(stream)))
+    T = np.eye(4)
+    T[:3] = np.array(list(res.rt)).reshape(3, 4)
+    return T, res
 
 
 def overlap(a_dev, b_dev, rt, radius=0.05, stream=None):

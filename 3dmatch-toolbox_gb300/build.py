@@ -35,7 +35,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xc
 EXTRA = os.environ.get("TDM_EXTRA_NVCC_FLAGS", "").split()
 # Translation units whose float results are compared bit for bit with the
 # CPU restatement: no multiply-add contraction on the device either.
-NO_FMAD = {"ransac.cu", "tsdf.cu", "batch.cu", "overlap.cu"}
+NO_FMAD = {"ransac.cu", "tsdf.cu", "batch.cu", "overlap.cu", "icp.cu"}
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + INC, "-I" + CSRC,
              "-I/usr/local/cuda/include"]
 

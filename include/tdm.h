@@ -219,6 +219,32 @@ size_t tdm_overlap_workspace_bytes(int32_t na, int32_t nb);
 tdm_status tdm_overlap(const float* a_dev, int32_t na, const float* b_dev, int32_t nb, const double rt_host[12],
                        float radius, int32_t* counts_dev, void* ws_dev, size_t ws_bytes, tdm_stream s);
 
+/* ---- ICP refinement: the step register2Fragments.m:70-78 leaves commented
+ * out (pcregrigid on 1 cm grid-averaged clouds, inlier ratio 0.3, tolerance
+ * [1e-4 m, 9e-5 deg], 50 iterations) ---------------------------------------- */
+typedef struct tdm_icp_params {
+  float grid;              /* grid-average cell, 0.01 */
+  float max_dist;          /* nearest-neighbour search radius, 0.10 */
+  float inlier_ratio;      /* closest fraction of the pairs kept, 0.30 */
+  int32_t max_iterations;  /* 50 */
+  float tol_translation;   /* 1e-4 (m) */
+  float tol_rotation_deg;  /* 9e-5 (degrees) */
+} tdm_icp_params;
+typedef struct tdm_icp_result {
+  double rt[12];           /* row-major 3x4, x_fixed = R x_moving + t */
+  int32_t iterations;
+  int32_t correspondences; /* pairs in the last fit */
+  float rmse;              /* of those pairs before the last update (m) */
+  int32_t converged;       /* 1 when the tolerances stopped it */
+} tdm_icp_result;
+/* Point-to-point ICP from init_rt (moving -> fixed).  Deterministic: exact
+ * integer Kabsch sums, ties broken by coordinates.  Clouds of 1 .. 524288
+ * points; synchronizes the stream once per iteration. */
+size_t tdm_icp_workspace_bytes(int32_t n_fixed, int32_t n_moving);
+tdm_status tdm_icp(const float* fixed_dev, int32_t n_fixed, const float* moving_dev, int32_t n_moving,
+                   const double init_rt_host[12], const tdm_icp_params* params, tdm_icp_result* result, void* ws_dev,
+                   size_t ws_bytes, tdm_stream s);
+
 /* ---- TSDF fusion: replaces depth-fusion/demo.cu:18-68 (Integrate) and
  * core/utils.hpp:23-65 (SaveVoxelGrid2SurfacePointCloud) -------------------- */
 /* tsdf = 1, weight = 0 (depth-fusion/demo.cu:131-135). */

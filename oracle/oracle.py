@@ -479,3 +479,55 @@ def evaluate_registration(result, gt, gt_info, err2=0.04):
                 if p <= err2:
                     good += 1
     return good / gt_num, (good / rs_num if rs_num else 0.0)
+
+
+# --------------------------------------------------------------------------
+# ICP (the register2Fragments.m:70-78 refinement): numpy FP64 restatement of
+# the library's algorithm, for parity tests.
+# --------------------------------------------------------------------------
+def _grid_average(p, cell):
+    k = np.floor(p.astype(np.float32) / np.float32(cell)).astype(np.int64)
+    _, inv, n = np.unique(k, axis=0, return_inverse=True, return_counts=True)
+    s = np.zeros((n.size, 3))
+    np.add.at(s, inv.ravel(), p.astype(np.float64))
+    return (s / n[:, None]).astype(np.float32)
+
+
+def icp(fixed, moving, init, grid=0.01, max_dist=0.10, inlier_ratio=0.30, iterations=1):
+    """Grid-average both clouds; per iteration: nearest fixed point within
+    max_dist of each moved point, the pairs in the 4,096-bin d^2 histogram
+    up to the bin reaching ceil(ratio * pairs), Kabsch (SVD) of those."""
+    from scipy.spatial import cKDTree
+    A, B = _grid_average(fixed, grid), _grid_average(moving, grid)
+    tree = cKDTree(A.astype(np.float64))
+    T = np.asarray(init, np.float64).reshape(-1)[:12].reshape(3, 4).copy()
+    md2 = np.float32(max_dist) * np.float32(max_dist)
+    for _ in range(iterations):
+        # moved points and squared distances in float32 with the library's
+        # operation order, so the histogram bins agree
+        Tf = T.astype(np.float32)
+        m = np.stack([((Tf[r, 0] * B[:, 0] + Tf[r, 1] * B[:, 1]) + Tf[r, 2] * B[:, 2]) + Tf[r, 3] for r in range(3)],
+                     1).astype(np.float32)
+        _, j = tree.query(m.astype(np.float64), distance_upper_bound=float(max_dist) * 1.001)
+        found = j < A.shape[0]
+        jj = np.where(found, j, 0)
+        e = m - A[jj]
+        d2 = (e[:, 0] * e[:, 0] + e[:, 1] * e[:, 1]) + e[:, 2] * e[:, 2]
+        ok = found & (d2 < md2)
+        if ok.sum() < 3:
+            break
+        b = np.minimum(4095, ((d2[ok] / md2) * np.float32(4096)).astype(np.int64))
+        hist = np.bincount(b, minlength=4096)
+        want = max(3, int(np.ceil(inlier_ratio * ok.sum())))
+        bmax = int(np.searchsorted(np.cumsum(hist), want))
+        sel = np.flatnonzero(ok)[b <= bmax]
+        x, y = A[jj[sel]].astype(np.float64), m[sel].astype(np.float64)
+        cx, cy = x.mean(0), y.mean(0)
+        U, _, Vt = np.linalg.svd((y - cy).T @ (x - cx))
+        D = np.diag([1.0, 1.0, np.sign(np.linalg.det(Vt.T @ U.T))])
+        R = Vt.T @ D @ U.T
+        t = cx - R @ cy
+        T = np.concatenate([R @ T[:, :3], (R @ T[:, 3] + t)[:, None]], 1)
+    out = np.eye(4)
+    out[:3] = T
+    return out
