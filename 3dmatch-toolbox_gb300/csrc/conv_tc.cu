@@ -703,6 +703,188 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
   }
 }
 
+// ---------------------------------------------------------------------------
+// conv1 with the im2col operand built in shared memory.  conv1 (1 input
+// channel, 27 taps) is a GEMM over the 28^3 output positions of each patch
+// with K = 27 taps padded to 32 and N = 64.  Instead of writing that operand
+// to HBM (1.4 MB per patch) and reading it back, four producer warps gather
+// the 27 FP32 taps of each row straight from the patch, convert them to BF16
+// and store the row into the K-major stage ([chunk][row][16 B]); the MMA and
+// epilogue roles are those of the generic kernel (N = 64, four 128-row
+// sub-tiles, two TMEM buffers), and the 4 KB of weights stay resident.
+// ---------------------------------------------------------------------------
+constexpr int kC1Prod = 4;                            // producer warps
+constexpr int kC1Threads = 32 * (kC1Prod + 1 + 4);    // + MMA warp + 4 epilogue warps
+constexpr int kC1Rows = 512;                          // rows per tile (4 sub-tiles)
+constexpr int kC1NSA = 3;                             // A stages
+constexpr uint32_t kC1Stage = 4u * kC1Rows * 16u;     // 32 KB
+constexpr uint32_t kC1W = 4u * 64u * 16u;             // weights: 4 chunks x 64 rows x 16 B
+
+struct C1Params {
+  const float* patches;
+  int64_t rows;  // B * 28^3
+  const uint8_t* wpk;
+  const float* bias;
+  uint8_t* out;
+  int64_t out_cs;
+  int64_t tiles;
+  int* err;
+};
+
+__global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params p) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t ACC = 4 * 64;  // one buffer: 4 sub-tiles x N 64
+  uint8_t* sW = smem;
+  uint8_t* sA = smem + kC1W;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sA + kC1NSA * kC1Stage);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * kC1NSA + 6);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (!__syncthreads_and(aborted(p.err) ? 0 : 1)) return;
+  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * kC1NSA;
+  const uint32_t wfull = emptyA + 8 * kC1NSA, accFull = wfull + 8, accEmpty = accFull + 16, done = accEmpty + 16;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kC1NSA; ++i) {
+      ptx::mbar_init(fullA + 8 * i, 32 * kC1Prod);  // every producer thread arrives
+      ptx::mbar_init(emptyA + 8 * i, 1);
+    }
+    ptx::mbar_init(wfull, 1);
+    for (int i = 0; i < 2; ++i) { ptx::mbar_init(accFull + 8 * i, 1); ptx::mbar_init(accEmpty + 8 * i, 4); }
+    ptx::mbar_init(done, 1);
+    ptx::fence_barrier_init();
+    ptx::fence_proxy_async_smem();
+  }
+  if (warp == kC1Prod) {
+    ptx::tmem_alloc(ptx::smem_u32(tmem_holder), 512);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  const uint32_t sA_u = ptx::smem_u32(sA), sW_u = ptx::smem_u32(sW);
+
+  if (warp < kC1Prod) {
+    // ---------------- producers: im2col rows into the stages ----------------
+    const int pt = threadIdx.x;  // 0 .. 127
+    if (pt == 0) {
+      ptx::mbar_arrive_expect_tx(wfull, kC1W);
+      ptx::bulk_g2s(sW_u, p.wpk, kC1W, wfull);
+    }
+    int sa = 0;
+    uint32_t pha = 0;
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
+      if (!wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+      uint8_t* st = sA + sa * kC1Stage;
+      for (int r = pt; r < kC1Rows; r += 32 * kC1Prod) {
+        const int64_t row = t * kC1Rows + r;
+        float v[32];
+        if (row < p.rows) {
+          const int64_t b = row / 21952;
+          const int q = (int)(row - b * 21952);
+          const int z = q / 784, y = (q / 28) % 28, x = q % 28;
+          const float* src = p.patches + b * 27000 + z * 900 + y * 30 + x;
+#pragma unroll
+          for (int tp = 0; tp < 27; ++tp) v[tp] = __ldg(src + (tp / 9) * 900 + ((tp / 3) % 3) * 30 + (tp % 3));
+        } else {
+#pragma unroll
+          for (int tp = 0; tp < 27; ++tp) v[tp] = 0.0f;
+        }
+#pragma unroll
+        for (int tp = 27; tp < 32; ++tp) v[tp] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          uint4 o;
+          o.x = pack_bf16x2(v[8 * j + 0], v[8 * j + 1]);
+          o.y = pack_bf16x2(v[8 * j + 2], v[8 * j + 3]);
+          o.z = pack_bf16x2(v[8 * j + 4], v[8 * j + 5]);
+          o.w = pack_bf16x2(v[8 * j + 6], v[8 * j + 7]);
+          *reinterpret_cast<uint4*>(st + ((size_t)j * kC1Rows + r) * 16) = o;
+        }
+      }
+      ptx::fence_proxy_async_smem();  // generic-proxy stores visible to the tensor core
+      mbar_arrive(fullA + 8 * sa);
+      if (++sa == kC1NSA) { sa = 0; pha ^= 1; }
+    }
+    if (pt == 0) wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_PRODUCER);
+  } else if (warp == kC1Prod) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      constexpr uint32_t idesc = ptx::make_idesc(64, 128, 1, 1);
+      constexpr uint32_t lboA = kC1Rows * 16u;
+      int sa = 0;
+      uint32_t pha = 0;
+      bool ok = wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_MMA);
+      uint32_t j = 0;
+      for (int64_t t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
+        const uint32_t buf = j & 1u, use = j >> 1;
+        if (!wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+        if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+        ptx::tc_fence_after();
+        const uint32_t aBase = sA_u + sa * kC1Stage, dbase = tmem + buf * ACC;
+#pragma unroll
+        for (int kk = 0; kk < 2; ++kk) {
+          const uint64_t bdesc = ptx::smem_desc(sW_u + (2 * kk) * 64 * 16, 64 * 16, 128);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const uint64_t adesc = ptx::smem_desc(aBase + (2 * kk) * lboA + (uint32_t)(i * 128) * 16u, lboA, 128);
+            ptx::mma_f16(dbase + i * 64, adesc, bdesc, idesc, kk > 0 ? 1u : 0u);
+          }
+        }
+        ptx::mma_commit(emptyA + 8 * sa);
+        if (++sa == kC1NSA) { sa = 0; pha ^= 1; }
+        ptx::mma_commit(accFull + 8 * buf);
+        ++j;
+      }
+      ptx::mma_commit(done);
+      wait_or_flag(done, 0, p.err, DEV_TIMEOUT_MMA);
+    }
+  } else {
+    // ---------------- epilogue: bias, ReLU, BF16 rows (conv2's chunk-planar input) ----------------
+    const int q = warp & 3;
+    uint32_t j = 0;
+    for (int64_t t = blockIdx.x; t < p.tiles; t += gridDim.x) {
+      const uint32_t buf = j & 1u, use = j >> 1;
+      const bool have =
+          __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0) != 0;
+      if (!have) break;
+      ptx::tc_fence_after();
+#pragma unroll 1
+      for (int i = 0; i < 4; ++i) {
+        const int64_t row = t * kC1Rows + i * 128 + q * 32 + lane;
+        const bool valid = row < p.rows;
+#pragma unroll 1
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+          float v[16];
+          ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC + (uint32_t)(i * 64 + c0), v);
+          if (!valid) continue;
+#pragma unroll
+          for (int e = 0; e < 16; ++e) v[e] = fmaxf(v[e] + __ldg(p.bias + c0 + e), 0.0f);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            uint4 o;
+            o.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
+            o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
+            o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
+            o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
+            *reinterpret_cast<uint4*>(p.out + (int64_t)(c0 / 8 + h) * p.out_cs + row * 16) = o;
+          }
+        }
+      }
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(accEmpty + 8 * buf);
+      ++j;
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == kC1Prod) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, 512);
+  }
+}
+
 int slab_rows(const TcLayer& L) {
   if (L.dxf) return (L.msub - 1) * kDxfSub + 128 + 2 * L.D;  // exact: three stages must fit beside the weights
   int r = L.msub * 128 + (L.nyx > 1 ? 2 * L.D + 2 : 0);
@@ -777,6 +959,36 @@ tdm_status launch_dxf(const KParams& kp, size_t smem, cudaStream_t s) {
 }
 
 }  // namespace
+
+// conv1 of B patches into conv2's chunk-planar BF16 input (out_cs bytes
+// between its 8 chunks); weights packed as the conv1 GEMM layer's.
+tdm_status launch_conv1_tc(const float* patches, int B, const TcLayer& L, uint8_t* out, int64_t out_cs,
+                           cudaStream_t s) {
+  TDM_REQUIRE(L.wpk && L.bias && L.nt == 64 && L.cin == 32, "conv1: weights not packed for the tensor-core form");
+  TDM_REQUIRE((reinterpret_cast<uintptr_t>(out) & 15) == 0 && (out_cs & 15) == 0, "conv1: output must be 16-byte aligned");
+  C1Params p;
+  p.patches = patches;
+  p.rows = (int64_t)B * 21952;
+  p.wpk = L.wpk;
+  p.bias = L.bias;
+  p.out = out;
+  p.out_cs = out_cs;
+  p.tiles = (p.rows + kC1Rows - 1) / kC1Rows;
+  p.err = device_error_word();
+  if (!p.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
+  if (p.rows == 0) return TDM_OK;
+  const size_t smem = kC1W + kC1NSA * kC1Stage + 256;
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [&] {
+    attr_err = cudaFuncSetAttribute(tc_conv1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  });
+  if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv1_kernel)");
+  const int64_t grid = std::min<int64_t>(p.tiles, sm_count());
+  tc_conv1_kernel<<<(unsigned)grid, kC1Threads, std::max<size_t>(smem, 120 * 1024), s>>>(p);
+  TDM_CHECK_LAUNCH("tc_conv1_kernel");
+  return TDM_OK;
+}
 
 #ifdef TDM_WAIT_STATS
 }  // namespace tdm

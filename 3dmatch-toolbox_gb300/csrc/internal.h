@@ -68,6 +68,10 @@ struct TcArgs {
 // Rows of slack a chunk-planar input needs after its last row for layer L.
 int64_t tc_tail_rows(const TcLayer& L);
 tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s);
+// conv1 with its im2col operand built in shared memory (L = the conv1 GEMM
+// layer's packed weights and bias); writes conv2's chunk-planar BF16 input.
+tdm_status launch_conv1_tc(const float* patches, int B, const TcLayer& L, uint8_t* out, int64_t out_cs,
+                           cudaStream_t s);
 // Whether layer L's (nt, msub) tile fits the shared-memory plan and TMEM.
 bool tc_layer_fits(const TcLayer& L);
 // Packs Marvin-layout weights [cout][cin][taps] (taps = nz*nyx, or the GEMM

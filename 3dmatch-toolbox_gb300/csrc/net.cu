@@ -380,7 +380,6 @@ Bf16Plan bf16_plan(const tdm_net* net, int B) {
   size_t b0 = 0, b1 = 0;
   for (int l : {1, 2, 4, 6, 8}) b0 = std::max(b0, (size_t)(l == 7 ? 1728 : chunks(l)) * P.rows_alloc[l] * 16);
   b1 = std::max(b1, (size_t)8 * ((int64_t)B * 17576 + 8) * 16);  // conv2 output (pre-pool)
-  b1 = std::max(b1, (size_t)4 * ((int64_t)B * 21952 + tc_tail_rows(net->tc[0])) * 16);  // conv1 im2col operand
   for (int l : {3, 5}) b1 = std::max(b1, (size_t)chunks(l) * P.rows_alloc[l] * 16);
   b1 = std::max(b1, (size_t)1728 * P.rows_alloc[7] * 16);  // conv7 -> conv8 flattened operand
   P.off1 = round16((int64_t)b0) + 4096;
@@ -416,23 +415,10 @@ tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, in
   Bf16Plan P = bf16_plan(net, B);
   uint8_t* b0 = net->ws;
   uint8_t* b1 = net->ws + P.off1;
-  // conv1 on tcgen05: im2col operand (in buffer 1) -> chunk-planar BF16 input of conv2
+  // conv1 on tcgen05, its im2col operand built in shared memory -> chunk-planar BF16 input of conv2
   int64_t cs = P.rows_alloc[1] * 16;
-  const int64_t rows1 = (int64_t)B * 21952;
-  const int64_t cs_i2c = (rows1 + tc_tail_rows(net->tc[0])) * 16;
   cudaEvent_t ev = net->begin(0, s);
-  tdm_status st = launch_im2col_conv1(patches, B, b1, cs_i2c, s);
-  if (st) return st;
-  {
-    TcArgs a{};
-    a.act = b1;
-    a.act_cs = cs_i2c;
-    a.rows = rows1;
-    a.out = b0;
-    a.out_cs = cs;
-    a.in_scale = a.out_qinv = 1.0f;
-    st = launch_tc_layer(net->tc[0], a, s);
-  }
+  tdm_status st = launch_conv1_tc(patches, B, net->tc[0], b0, cs, s);
   net->end(ev, s);
   if (st) return st;
   if (stop == 0) return c8_response(b0, cs, B, 0, false, desc, s);
@@ -719,9 +705,9 @@ std::vector<Tile> tile_candidates(tdm_net* net, int l) {
     }
     return out;
   }
+  if (l == 0) return {Tile{64, 4}};  // conv1's fused im2col kernel has one tile shape
   for (const Tile& t : kTiles) {
     TcLayer L = active_layer(net, l);
-    if (l == 0 && t.nt != 64) continue;
     L.nt = t.nt;
     L.msub = t.msub;
     if (tc_layer_fits(L)) out.push_back(t);
