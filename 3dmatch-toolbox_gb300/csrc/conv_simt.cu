@@ -240,31 +240,6 @@ __global__ __launch_bounds__(256) void pool_c8_kernel(const uint8_t* __restrict_
   *reinterpret_cast<uint4*>(out + (int64_t)j * out_cs + q * 16) = o;
 }
 
-// conv1 operand for the tensor cores: for every output position of the 28^3
-// grid, its 27 input taps (z,y,x order, as Marvin's [64][1][3][3][3] filter)
-// padded to 32 and rounded to BF16, as 4 chunk-planar 16-byte chunks.
-__global__ __launch_bounds__(256) void im2col_conv1_kernel(const float* __restrict__ patches, int64_t n_pos,
-                                                           uint8_t* __restrict__ out, int64_t out_cs) {
-  const int64_t pos = (int64_t)blockIdx.x * 256 + threadIdx.x;
-  if (pos >= n_pos) return;
-  const int64_t b = pos / 21952;
-  const int r = (int)(pos - b * 21952);
-  const int z = r / 784, y = (r / 28) % 28, x = r % 28;
-  const float* p = patches + b * 27000 + z * 900 + y * 30 + x;
-  float v[32];
-#pragma unroll
-  for (int t = 0; t < 27; ++t) v[t] = __ldg(p + (t / 9) * 900 + ((t / 3) % 3) * 30 + (t % 3));
-#pragma unroll
-  for (int t = 27; t < 32; ++t) v[t] = 0.0f;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    __nv_bfloat162 h[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) h[e] = __floats2bfloat162_rn(v[8 * j + 2 * e], v[8 * j + 2 * e + 1]);
-    *reinterpret_cast<uint4*>(out + (int64_t)j * out_cs + pos * 16) = *reinterpret_cast<uint4*>(h);
-  }
-}
-
 // Same pool on the E4M3 chunk-planar layout (16 channels per 16-byte row).
 // Inputs are ReLU outputs (>= 0), whose E4M3 bytes order like the values, so
 // a byte-wise unsigned max is the max-pool.
@@ -303,13 +278,6 @@ tdm_status launch_pool_c16_u8(const uint8_t* in, int64_t in_cs, int B, int D, in
   int64_t n = n_out * nchunks;
   pool_c16_u8_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, in_cs, D, nchunks, n_out, out, out_cs);
   TDM_CHECK_LAUNCH("pool_c16_u8_kernel");
-  return TDM_OK;
-}
-
-tdm_status launch_im2col_conv1(const float* patches, int B, uint8_t* out, int64_t out_cs, cudaStream_t s) {
-  int64_t n_pos = (int64_t)B * 21952;
-  im2col_conv1_kernel<<<(unsigned)((n_pos + 255) / 256), 256, 0, s>>>(patches, n_pos, out, out_cs);
-  TDM_CHECK_LAUNCH("im2col_conv1_kernel");
   return TDM_OK;
 }
 

@@ -14,7 +14,6 @@ namespace tdm {
 tdm_status launch_conv1(const float* patches, int B, const float* w, const float* bias, bool bf16_out, void* out,
                         int64_t out_cs, cudaStream_t s);
 // BF16 tensor-core form of conv1: 27 taps (padded to 32) per output position.
-tdm_status launch_im2col_conv1(const float* patches, int B, uint8_t* out, int64_t out_cs, cudaStream_t s);
 tdm_status launch_conv_f32(const float* in, int B, int D, int C, int ks, const float* w, const float* bias, int K,
                            bool relu, float* out, cudaStream_t s);
 tdm_status launch_pool_f32(const float* in, int B, int D, int C, float* out, cudaStream_t s);
