@@ -40,7 +40,7 @@ EXPORTS = [
     "tdm_pipeline_create", "tdm_pipeline_destroy", "tdm_describe_fragment", "tdm_register_pair",
     "tdm_register_pair_host", "tdm_net_clone", "tdm_net_workspace_bytes",
     "tdm_server_create", "tdm_server_slots", "tdm_server_submit", "tdm_server_wait", "tdm_server_destroy",
-    "tdm_net_autotune", "tdm_net_tiles", "tdm_net_set_tile",
+    "tdm_net_autotune", "tdm_net_tiles", "tdm_net_set_tile", "tdm_net_tile_forms", "tdm_net_set_tile_form",
     "tdm_batch_create", "tdm_batch_destroy", "tdm_batch_device_bytes", "tdm_describe_batch", "tdm_batch_stats",
     "tdm_overlap_workspace_bytes", "tdm_overlap", "tdm_tdf_exact", "tdm_icp_workspace_bytes", "tdm_icp",
 ]
@@ -166,6 +166,8 @@ def lib():
         "tdm_net_autotune": (i32, [P, P, i32, i32, P]),
         "tdm_net_tiles": (i32, [P, P, P]),
         "tdm_net_set_tile": (i32, [P, i32, i32, i32]),
+        "tdm_net_tile_forms": (i32, [P, P]),
+        "tdm_net_set_tile_form": (i32, [P, i32, i32, i32, i32]),
         "tdm_batch_create": (i32, [ctypes.POINTER(BatchConfig), P, ctypes.POINTER(P)]),
         "tdm_batch_destroy": (i32, [P]),
         "tdm_batch_device_bytes": (sz, [P]),
@@ -354,8 +356,21 @@ class Net:
         check(lib().tdm_net_tiles(self.handle, _ptr(nt), _ptr(ms)))
         return {k: (int(nt[i]), int(ms[i])) for i, k in enumerate(self.LAYER_SLOTS[:9])}
 
-    def set_tile(self, layer: str, nt: int, msub: int) -> None:
-        check(lib().tdm_net_set_tile(self.handle, self.LAYER_SLOTS.index(layer), nt, msub))
+    CONV_FORMS = ("grid", "dxf", "gather")
+
+    def forms(self) -> dict:
+        """{layer: kernel form}: "grid" (implicit GEMM over every input
+        position), "dxf" (conv2's dx-fused form) or "gather" (GEMM over the
+        valid output positions, A rows gathered per tap)."""
+        f = np.zeros(9, np.int32)
+        check(lib().tdm_net_tile_forms(self.handle, _ptr(f)))
+        return {k: self.CONV_FORMS[int(f[i])] for i, k in enumerate(self.LAYER_SLOTS[:9])}
+
+    def set_tile(self, layer: str, nt: int, msub: int, form: str = None) -> None:
+        """Tile (and optionally kernel form) of one layer; without a form the
+        layer keeps its current form when that form has the tile."""
+        code = -1 if form is None else self.CONV_FORMS.index(form)
+        check(lib().tdm_net_set_tile_form(self.handle, self.LAYER_SLOTS.index(layer), nt, msub, code))
 
     def close(self):
         if self.handle:

@@ -382,6 +382,278 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
 }
 
 // ---------------------------------------------------------------------------
+// Gathered-row form of a 3x3x3 conv (conv3..conv7).
+//
+// The grid form above computes a GEMM row for every input position and drops
+// the rows with x, y or z >= Do in its epilogue: 1.65x (conv3) to 4.6x (conv7)
+// the useful MACs.  Here M runs over the valid output positions only, row
+// m = ((b*Do + z)*Do + y)*Do + x, and four gather warps build each tap's A
+// operand row by row: the 16-byte chunks of input position
+// ((b*D + z+dz)*D + y+dy)*D + x+dx go by cp.async straight into the K-major
+// stage layout [chunk][row][16 B].  A stage is one (tap, K group).  The weight
+// stages (the grid form's packing), the MMA issue and the TMEM epilogue are the
+// grid form's, and taps and K groups run in the same order, so every output is
+// the same sum taken in the same order.
+// ---------------------------------------------------------------------------
+constexpr int kGWarps = 4;                          // gather warps (warps 6..9)
+constexpr int kGThreads = kThreads + 32 * kGWarps;
+constexpr int kGNSA = 4;                            // A stages
+constexpr int kGDepth = 3;                          // stages a gather thread keeps in flight
+
+// 16-byte global -> shared copy; src_bytes = 0 writes zeros without reading.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <int NT, int MSUB, bool FP8>
+__global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KParams p) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr int MCTA = MSUB * 128;
+  constexpr uint32_t ACC_COLS = MSUB * NT;
+  constexpr int NBUF = 2 * ACC_COLS <= 512 ? 2 : 1;  // accumulator buffers
+  constexpr uint32_t TMEM_COLS = tmem_cols_for(NBUF * ACC_COLS);
+  static_assert(ACC_COLS <= 512, "the accumulator must fit in TMEM");
+  constexpr int E = FP8 ? 16 : 8;  // channels per 16-byte chunk
+  const int nsb = p.nsb, cpg = p.cpg;
+  const uint32_t a_stage = 16u * (uint32_t)cpg * MCTA;
+  constexpr uint32_t b_stage = NT * 128u;
+  uint8_t* sB = smem + kGNSA * a_stage;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + (size_t)nsb * b_stage);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * kGNSA + 2 * MAX_NSB + 5);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (!__syncthreads_and(aborted(p.err) ? 0 : 1)) return;  // another CTA already failed
+
+  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * kGNSA;
+  const uint32_t fullB = emptyA + 8 * kGNSA, emptyB = fullB + 8 * MAX_NSB;
+  const uint32_t accFull = emptyB + 8 * MAX_NSB, accEmpty = accFull + 16, done = accEmpty + 16;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kGNSA; ++i) {
+      ptx::mbar_init(fullA + 8 * i, 32 * kGWarps);  // every gather thread arrives
+      ptx::mbar_init(emptyA + 8 * i, 1);
+    }
+    for (int i = 0; i < nsb; ++i) { ptx::mbar_init(fullB + 8 * i, 1); ptx::mbar_init(emptyB + 8 * i, 1); }
+    for (int i = 0; i < 2; ++i) { ptx::mbar_init(accFull + 8 * i, 1); ptx::mbar_init(accEmpty + 8 * i, 4); }
+    ptx::mbar_init(done, 1);
+    ptx::fence_barrier_init();
+    ptx::fence_proxy_async_smem();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(ptx::smem_u32(tmem_holder), TMEM_COLS);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  const uint32_t sA_u = ptx::smem_u32(smem), sB_u = ptx::smem_u32(sB);
+  const int Do2 = p.Do * p.Do, Do3 = Do2 * p.Do;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- weight producer ----------------
+      int sb = 0;
+      uint32_t phb = 0;
+      int armedB[MAX_NSB];
+      for (int i = 0; i < MAX_NSB; ++i) armedB[i] = -1;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+        const int nt = (int)(t % p.ntiles);
+        for (int zt = 0; zt < p.nz && ok; ++zt)
+          for (int cg = 0; cg < p.kgroups && ok; ++cg)
+            for (int yx = 0; yx < p.nyx; ++yx) {
+              if (!wait_or_flag(emptyB + 8 * sb, phb ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+              ptx::mbar_arrive_expect_tx(fullB + 8 * sb, b_stage);
+              armedB[sb] = (int)phb;
+              const int64_t blk = (((int64_t)nt * p.nz + zt) * p.kgroups + cg) * p.nyx + yx;
+              ptx::bulk_g2s(sB_u + sb * b_stage, p.wpk + blk * b_stage, b_stage, fullB + 8 * sb);
+              if (++sb == nsb) { sb = 0; phb ^= 1; }
+            }
+      }
+      for (int i = 0; i < nsb; ++i)
+        if (armedB[i] >= 0) wait_or_flag(fullB + 8 * i, (uint32_t)armedB[i], p.err, DEV_TIMEOUT_PRODUCER);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      constexpr uint32_t idesc = FP8 ? ptx::make_idesc(NT, 128, 0, 0) : ptx::make_idesc(NT, 128, 1, 1);
+      constexpr uint32_t lboA = MCTA * 16u;
+      int sa = 0, sb = 0;
+      uint32_t pha = 0, phb = 0;
+      bool ok = true;
+      uint32_t j = 0;  // tiles done by this CTA
+      for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+        const uint32_t buf = j % NBUF, use = j / NBUF;
+        if (!wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA)) break;
+        ptx::tc_fence_after();
+        const uint32_t dbase = tmem + buf * ACC_COLS;
+        uint32_t accumulate = 0;
+        for (int zt = 0; zt < p.nz && ok; ++zt)
+          for (int cg = 0; cg < p.kgroups && ok; ++cg)
+            for (int yx = 0; yx < p.nyx; ++yx) {
+              if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA) ||
+                  !wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA)) {
+                ok = false;
+                break;
+              }
+              ptx::tc_fence_after();
+              const uint32_t aBase = sA_u + sa * a_stage, bBase = sB_u + sb * b_stage;
+              for (int kk = 0; kk < cpg / 2; ++kk) {
+                const uint64_t bdesc = ptx::smem_desc(bBase + (2 * kk) * NT * 16, NT * 16, 128);
+#pragma unroll
+                for (int i = 0; i < MSUB; ++i) {
+                  const uint64_t adesc = ptx::smem_desc(aBase + (2 * kk) * lboA + (uint32_t)(i * 128) * 16u, lboA, 128);
+                  if (FP8) ptx::mma_f8(dbase + i * NT, adesc, bdesc, idesc, accumulate);
+                  else ptx::mma_f16(dbase + i * NT, adesc, bdesc, idesc, accumulate);
+                }
+                accumulate = 1;
+              }
+              ptx::mma_commit(emptyB + 8 * sb);
+              if (++sb == nsb) { sb = 0; phb ^= 1; }
+              ptx::mma_commit(emptyA + 8 * sa);
+              if (++sa == kGNSA) { sa = 0; pha ^= 1; }
+            }
+        ptx::mma_commit(accFull + 8 * buf);  // fires when this tile's MMAs are complete
+        ++j;
+      }
+      ptx::mma_commit(done);
+      wait_or_flag(done, 0, p.err, DEV_TIMEOUT_MMA);
+    }
+  } else if (warp < 6) {
+    // ---------------- epilogue (warps 2-5: TMEM lane quarter warp % 4) ----------------
+    const int q = warp & 3;
+    uint32_t j = 0;
+    for (int64_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
+      const int64_t m0 = (t / p.ntiles) * MCTA;
+      const int n0 = (int)(t % p.ntiles) * NT;
+      const uint32_t buf = j % NBUF, use = j / NBUF;
+      const bool have =
+          __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0) != 0;
+      if (!have) break;
+      ptx::tc_fence_after();
+#pragma unroll 1
+      for (int i = 0; i < MSUB; ++i) {
+        const int64_t row = m0 + i * 128 + q * 32 + lane;
+        const bool valid = row < p.rows;
+        const int64_t b = row / Do3;
+        const int tap = (int)(row - b * Do3);
+#pragma unroll 1
+        for (int c0 = 0; c0 < NT; c0 += 16) {
+          float v[16];
+          ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)(i * NT + c0), v);
+          if (!valid) continue;
+          const int n = n0 + c0;
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            float a = v[e];
+            if (FP8) a = a * (p.in_scale * __ldg(p.wscale + n + e));
+            a += __ldg(p.bias + n + e);
+            if (p.relu) a = fmaxf(a, 0.0f);
+            v[e] = a;
+          }
+          // chunk-planar output: next layer's input grid (row = position) or
+          // conv8's operand (chunk = tap * Cout/E + channel chunk, row = patch)
+          const bool taps = p.out_mode == TC_OUT_C8_TAPS;
+          const int64_t chunk0 = (taps ? (int64_t)tap * (p.cout / E) : 0) + n / E;
+          const int64_t prow = taps ? b : row;
+          if (FP8) {
+            uint4 o;
+            o.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
+            o.y = pack_e4m3x4(v[4] * p.out_qinv, v[5] * p.out_qinv, v[6] * p.out_qinv, v[7] * p.out_qinv);
+            o.z = pack_e4m3x4(v[8] * p.out_qinv, v[9] * p.out_qinv, v[10] * p.out_qinv, v[11] * p.out_qinv);
+            o.w = pack_e4m3x4(v[12] * p.out_qinv, v[13] * p.out_qinv, v[14] * p.out_qinv, v[15] * p.out_qinv);
+            *reinterpret_cast<uint4*>(p.out + chunk0 * p.out_cs + prow * 16) = o;
+          } else {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              uint4 o;
+              o.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
+              o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
+              o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
+              o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
+              *reinterpret_cast<uint4*>(p.out + (chunk0 + h) * p.out_cs + prow * 16) = o;
+            }
+          }
+        }
+      }
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(accEmpty + 8 * buf);
+      ++j;
+    }
+  } else {
+    // ---------------- gather warps: each tap's A rows into the stages ----------------
+    const int gt = threadIdx.x - kThreads;  // 0 .. 127: row gt of every 128-row sub-tile
+    int sa = 0;
+    uint32_t pha = 0;
+    int pend[kGDepth];  // stages copied but not yet published, oldest first from q0
+    int q0 = 0, np = 0;
+    bool ok = true;
+    const int64_t plane = (int64_t)p.D * p.D;
+    for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+      const int64_t m0 = (t / p.ntiles) * MCTA;
+      int64_t base[MSUB];
+      uint32_t bytes[MSUB];
+#pragma unroll
+      for (int i = 0; i < MSUB; ++i) {
+        const int64_t row = m0 + i * 128 + gt;
+        base[i] = 0;
+        bytes[i] = 0;  // rows past the end are zero-filled
+        if (row < p.rows) {
+          const int64_t b = row / Do3;
+          const int r = (int)(row - b * Do3);
+          const int z = r / Do2, y = (r / p.Do) % p.Do, x = r % p.Do;
+          base[i] = ((b * p.D + z) * p.D + y) * p.D + x;
+          bytes[i] = 16;
+        }
+      }
+      for (int zt = 0; zt < p.nz && ok; ++zt)
+        for (int cg = 0; cg < p.kgroups && ok; ++cg)
+          for (int yx = 0; yx < p.nyx; ++yx) {
+            if (!wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+            const int64_t off = zt * plane + (yx / 3) * p.D + (yx % 3);
+            const uint32_t dst = sA_u + sa * a_stage + gt * 16;
+            const uint8_t* cbase = p.act + (int64_t)cg * cpg * p.act_cs;
+#pragma unroll
+            for (int i = 0; i < MSUB; ++i) {
+              const uint8_t* src = cbase + (base[i] + off) * 16;
+#pragma unroll 4
+              for (int c = 0; c < cpg; ++c)
+                cp_async16(dst + (uint32_t)(c * MCTA + i * 128) * 16u, src + c * p.act_cs, bytes[i]);
+            }
+            cp_async_commit();
+            pend[(q0 + np) % kGDepth] = sa;
+            if (++np == kGDepth) {  // publish the oldest stage once its copies have landed
+              cp_async_wait<kGDepth - 1>();
+              ptx::fence_proxy_async_smem();  // generic-proxy writes visible to the tensor core
+              mbar_arrive(fullA + 8 * pend[q0]);
+              q0 = (q0 + 1) % kGDepth;
+              --np;
+            }
+            if (++sa == kGNSA) { sa = 0; pha ^= 1; }
+          }
+    }
+    cp_async_wait<0>();  // no copy may still be in flight when the CTA exits
+    ptx::fence_proxy_async_smem();
+    for (; np > 0; --np) {
+      mbar_arrive(fullA + 8 * pend[q0]);
+      q0 = (q0 + 1) % kGDepth;
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // dx-fused form of a 3x3x3 conv with 64 BF16 inputs and 64 outputs (conv2).
 //
 // An N = 64 MMA reads its A rows (4 KB per 128 x 16) and B (2 KB) from
@@ -900,14 +1172,20 @@ int chunks_per_group(const TcLayer& L) {
 
 size_t a_stage_bytes(const TcLayer& L) { return (size_t)16 * chunks_per_group(L) * slab_rows(L); }
 
+// gathered-row form: one (tap, K group) of msub*128 rows per A stage
+size_t gather_stage_bytes(const TcLayer& L) { return (size_t)16 * chunks_per_group(L) * L.msub * 128; }
+
 int weight_stages(const TcLayer& L) {
-  size_t left = kSmemLimit - kSmemReserve - NSA * a_stage_bytes(L);
+  const size_t a = L.gather ? kGNSA * gather_stage_bytes(L) : NSA * a_stage_bytes(L);
+  if (a + kSmemReserve >= kSmemLimit) return 0;
+  size_t left = kSmemLimit - kSmemReserve - a;
   int n = (int)(left / ((size_t)L.nt * 128));
   return n < MAX_NSB ? n : MAX_NSB;
 }
 
 size_t smem_bytes(const TcLayer& L) {
   if (L.dxf) return kDxfWBytes + kDxfNSA * a_stage_bytes(L) + kDxfXchg + kDxfStage + 32 + kSmemReserve;
+  if (L.gather) return kGNSA * gather_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
   return NSA * a_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
 }
 
@@ -939,6 +1217,27 @@ tdm_status launch_t(const KParams& kp, size_t smem, cudaStream_t s) {
   kern<<<(unsigned)std::max<int64_t>(grid, 1), kThreads, req, s>>>(kp);
   TDM_CHECK_LAUNCH("tc_conv_kernel");
   return TDM_OK;
+}
+
+template <int NT, int MSUB, bool FP8>
+tdm_status launch_g(const KParams& kp, size_t smem, cudaStream_t s) {
+  auto kern = tc_conv_gather_kernel<NT, MSUB, FP8>;
+  size_t req = std::max<size_t>(smem, 120 * 1024);
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [&] {
+    attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  });
+  if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_gather_kernel)");
+  int64_t grid = std::min<int64_t>(kp.total_tiles, sm_count());
+  kern<<<(unsigned)std::max<int64_t>(grid, 1), kGThreads, req, s>>>(kp);
+  TDM_CHECK_LAUNCH("tc_conv_gather_kernel");
+  return TDM_OK;
+}
+
+// (N tile, M sub-tiles) shapes the gathered-row kernel is built for
+bool gather_tile_built(int nt, int msub) {
+  return (nt == 256 && (msub == 1 || msub == 2)) || (nt == 128 && msub == 2);
 }
 
 template <int MSUB, bool FP8_OUT>
@@ -1011,6 +1310,9 @@ bool tc_layer_fits(const TcLayer& L) {
   if (L.dxf)
     return L.nt == kDxfNt && (L.msub == 1 || L.msub == 2) && L.cin == 64 && L.cout == 2 * kDxfNt && L.nz == 3 &&
            L.nyx == 9 && !L.fp8_in && smem_bytes(L) <= kSmemLimit;
+  if (L.gather)
+    return L.nz == 3 && L.nyx == 9 && L.fp8_in == L.fp8_out && gather_tile_built(L.nt, L.msub) &&
+           L.cout % L.nt == 0 && weight_stages(L) >= 2 && smem_bytes(L) <= kSmemLimit;
   return L.nt > 0 && L.msub > 0 && L.cout % L.nt == 0 && 2 * L.msub * L.nt <= 512 && weight_stages(L) >= 2 &&
          smem_bytes(L) <= kSmemLimit;
 }
@@ -1052,6 +1354,25 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
     const size_t smem = smem_bytes(L);
     if (L.msub == 2) return L.fp8_out ? launch_dxf<2, true>(kp, smem, s) : launch_dxf<2, false>(kp, smem, s);
     return L.fp8_out ? launch_dxf<1, true>(kp, smem, s) : launch_dxf<1, false>(kp, smem, s);
+  }
+  if (L.gather) {
+    TDM_REQUIRE(tc_layer_fits(L), "tc layer: unsupported gathered-row tile");
+    TDM_REQUIRE((reinterpret_cast<uintptr_t>(a.act) & 15) == 0 && (a.act_cs & 15) == 0 &&
+                    (reinterpret_cast<uintptr_t>(L.wpk) & 15) == 0,
+                "tc layer: operands must be 16-byte aligned");
+    const int64_t D3 = (int64_t)L.D * L.D * L.D;
+    TDM_REQUIRE(a.rows % D3 == 0, "tc layer: input rows must be whole patches");
+    kp.rows = a.rows / D3 * L.Do * L.Do * L.Do;  // M = valid output positions
+    if (kp.rows == 0) return TDM_OK;
+    kp.nsb = weight_stages(L);
+    const int64_t mcta = (int64_t)L.msub * 128;
+    kp.ntiles = L.cout / L.nt;
+    kp.total_tiles = ((kp.rows + mcta - 1) / mcta) * kp.ntiles;
+    const size_t smem = smem_bytes(L);
+    const bool f8 = L.fp8_in;
+    if (L.nt == 256 && L.msub == 2) return f8 ? launch_g<256, 2, true>(kp, smem, s) : launch_g<256, 2, false>(kp, smem, s);
+    if (L.nt == 256 && L.msub == 1) return f8 ? launch_g<256, 1, true>(kp, smem, s) : launch_g<256, 1, false>(kp, smem, s);
+    return f8 ? launch_g<128, 2, true>(kp, smem, s) : launch_g<128, 2, false>(kp, smem, s);
   }
   kp.nsb = weight_stages(L);
   TDM_REQUIRE(kp.nsb >= 2, "tc layer: shared-memory plan leaves fewer than 2 weight stages");

@@ -48,6 +48,10 @@ struct TcLayer {
   // two rows; nt = 32 output channels per CTA (two halves), weights resident
   // in shared memory, msub sub-tiles of 128 rows giving 126 outputs each.
   bool dxf = false;
+  // gathered-row form (3x3x3 convs): M runs over the valid output positions
+  // only and gather warps copy each tap's A rows into shared memory, instead
+  // of the grid form's rows for every input position.
+  bool gather = false;
   // device data
   uint8_t* wpk;   // packed weights, blocks [ntile][zt][cg][yx] of nt*128 bytes
   float* bias;    // [cout]

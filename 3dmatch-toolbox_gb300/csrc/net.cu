@@ -203,6 +203,11 @@ TcLayer make_tc_layer(int l, bool use_feat) {
     L.nt = 32;
     L.msub = 2;
   }
+  if (l >= 4 && l <= 6) {  // conv5..conv7: M over the valid output positions only
+    L.gather = true;
+    L.nt = 256;
+    L.msub = 2;
+  }
   return L;
 }
 
@@ -684,9 +689,13 @@ uint64_t net_generation(const tdm_net* net) { return net->generation; }
 namespace {
 
 struct Tile {
-  int nt, msub;
+  int nt, msub, form;  // form: TDM_CONV_GRID, TDM_CONV_DXF or TDM_CONV_GATHER
 };
-constexpr Tile kTiles[] = {{64, 4}, {64, 2}, {128, 2}, {128, 1}, {256, 1}};
+constexpr Tile kTiles[] = {{64, 4, TDM_CONV_GRID},   {64, 2, TDM_CONV_GRID},    {128, 2, TDM_CONV_GRID},
+                           {128, 1, TDM_CONV_GRID},  {256, 1, TDM_CONV_GRID},   {256, 2, TDM_CONV_GATHER},
+                           {256, 1, TDM_CONV_GATHER}, {128, 2, TDM_CONV_GATHER}};
+
+int form_of(const TcLayer& L) { return L.dxf ? TDM_CONV_DXF : L.gather ? TDM_CONV_GATHER : TDM_CONV_GRID; }
 
 // The tcgen05 layer a forward of `net` runs for layer l.
 TcLayer& active_layer(tdm_net* net, int l) {
@@ -701,15 +710,16 @@ std::vector<Tile> tile_candidates(tdm_net* net, int l) {
     for (int ms : {2, 1}) {
       TcLayer L = active_layer(net, l);
       L.msub = ms;
-      if (tc_layer_fits(L)) out.push_back(Tile{32, ms});
+      if (tc_layer_fits(L)) out.push_back(Tile{32, ms, TDM_CONV_DXF});
     }
     return out;
   }
-  if (l == 0) return {Tile{64, 4}};  // conv1's fused im2col kernel has one tile shape
+  if (l == 0) return {Tile{64, 4, TDM_CONV_GRID}};  // conv1's fused im2col kernel has one tile shape
   for (const Tile& t : kTiles) {
     TcLayer L = active_layer(net, l);
     L.nt = t.nt;
     L.msub = t.msub;
+    L.gather = t.form == TDM_CONV_GATHER;
     if (tc_layer_fits(L)) out.push_back(t);
   }
   return out;
@@ -739,9 +749,10 @@ tdm_status set_tile(tdm_net* net, int l, Tile t) {
       L.wpk = d;
     }
   }
-  if (L.nt != t.nt || L.msub != t.msub) ++net->generation;
+  if (L.nt != t.nt || L.msub != t.msub || form_of(L) != t.form) ++net->generation;
   L.nt = t.nt;
   L.msub = t.msub;
+  if (!L.dxf) L.gather = t.form == TDM_CONV_GATHER;
   return TDM_OK;
 }
 
@@ -802,15 +813,33 @@ extern "C" tdm_status tdm_net_tiles(const tdm_net* net, int32_t nt[9], int32_t m
   return TDM_OK;
 }
 
-extern "C" tdm_status tdm_net_set_tile(tdm_net* net, int32_t layer, int32_t nt, int32_t msub) {
+extern "C" tdm_status tdm_net_tile_forms(const tdm_net* net, int32_t form[9]) {
+  TDM_REQUIRE(net && form, "tdm_net_tile_forms: null pointer");
+  for (int l = 0; l < 9; ++l) {
+    const TcLayer& L = (net->prec == TDM_FP8 && l >= 1 && l <= 7) ? net->tc8[l] : net->tc[l];
+    form[l] = net->prec == TDM_FP32 ? TDM_CONV_GRID : form_of(L);
+  }
+  return TDM_OK;
+}
+
+extern "C" tdm_status tdm_net_set_tile_form(tdm_net* net, int32_t layer, int32_t nt, int32_t msub, int32_t form) {
   TDM_REQUIRE(net && layer >= 0 && layer < 9, "tdm_net_set_tile: bad arguments");
   TDM_REQUIRE(net->prec != TDM_FP32, "tdm_net_set_tile: the FP32 form has no tile choice");
-  for (const Tile& t : tile_candidates(net, layer))
-    if (t.nt == nt && t.msub == msub) {
+  // an explicit form first; else the layer's current form, then any form with this tile
+  const int cur = form_of(active_layer(net, layer));
+  const std::vector<Tile> cand = tile_candidates(net, layer);
+  for (int pass = 0; pass < 2; ++pass)
+    for (const Tile& t : cand) {
+      if (t.nt != nt || t.msub != msub) continue;
+      if (form >= 0 ? t.form != form : (pass == 0 && t.form != cur)) continue;
       TDM_CHECK_CUDA(cudaDeviceSynchronize());  // no forward may still read the old packing's tile
       return set_tile(net, layer, t);
     }
   return fail(TDM_ERR_INVALID_ARG, "tdm_net_set_tile: tile not available for this layer");
+}
+
+extern "C" tdm_status tdm_net_set_tile(tdm_net* net, int32_t layer, int32_t nt, int32_t msub) {
+  return tdm_net_set_tile_form(net, layer, nt, msub, -1);
 }
 
 extern "C" tdm_status tdm_net_destroy(tdm_net* net) {

@@ -150,8 +150,18 @@ tdm_status tdm_net_autotune(tdm_net* net, const float* patches_dev, int32_t b, i
 /* Current tile per layer (0..8 = conv1..feat; 0 for the FP32 form). */
 tdm_status tdm_net_tiles(const tdm_net* net, int32_t nt[9], int32_t msub[9]);
 /* Sets one layer's tile by hand (nt in {64,128,256} dividing the layer's
- * outputs, msub M sub-tiles of 128 rows, 2*msub*nt <= 512 TMEM columns). */
+ * outputs, msub M sub-tiles of 128 rows, 2*msub*nt <= 512 TMEM columns in the
+ * grid form), keeping the layer's kernel form when it has that tile. */
 tdm_status tdm_net_set_tile(tdm_net* net, int32_t layer, int32_t nt, int32_t msub);
+/* Kernel form of a tensor-core layer.  GRID: implicit GEMM over every input
+ * position (rows with x, y or z >= Do computed and dropped); DXF: conv2's
+ * dx-fused form; GATHER: GEMM over the valid output positions only, each
+ * tap's A rows gathered into shared memory (3x3x3 convs conv3..conv7; tiles
+ * (256,2), (256,1), (128,2)).  All forms give the same bits. */
+typedef enum { TDM_CONV_GRID = 0, TDM_CONV_DXF = 1, TDM_CONV_GATHER = 2 } tdm_conv_form;
+tdm_status tdm_net_tile_forms(const tdm_net* net, int32_t form[9]);
+/* Sets tile and form (-1: the current form if it has the tile, else any). */
+tdm_status tdm_net_set_tile_form(tdm_net* net, int32_t layer, int32_t nt, int32_t msub, int32_t form);
 tdm_status tdm_net_destroy(tdm_net* net);
 /* Seeded He-normal weights (N(0, 2/fan_in)), uniform biases in [-0.05, 0.05],
  * written as float32 .marvin records. */

@@ -139,10 +139,15 @@ def test_autotune_keeps_descriptor_bits(tdm, weights, patches, precision):
         net.calibrate(patches)
     before = net.forward(patches).cpu().numpy()
     tiles = net.autotune(patches, reps=2)
+    forms = net.forms()
     for layer, (nt, ms) in tiles.items():
         if layer == "conv2":  # dx-fused: 32 outputs per CTA, N = 96
-            assert nt == 32 and ms in (1, 2), layer
+            assert forms[layer] == "dxf" and nt == 32 and ms in (1, 2), layer
+        elif forms[layer] == "gather":  # one accumulator buffer allowed
+            assert layer in ("conv3", "conv4", "conv5", "conv6", "conv7"), layer
+            assert (nt, ms) in ((256, 2), (256, 1), (128, 2)), layer
         else:
+            assert forms[layer] == "grid", layer
             assert nt in (64, 128, 256) and ms in (1, 2, 4) and 2 * nt * ms <= 512, layer
     after = net.forward(patches).cpu().numpy()
     assert np.array_equal(before, after)
@@ -150,14 +155,38 @@ def test_autotune_keeps_descriptor_bits(tdm, weights, patches, precision):
 
 
 @pytest.mark.parametrize("layer,tiles", [("conv2", [(32, 2), (32, 1)]),
-                                         ("conv3", [(64, 4), (64, 2), (128, 2), (128, 1)]),
-                                         ("conv6", [(64, 2), (128, 1), (256, 1)]),
+                                         ("conv3", [(64, 4), (64, 2), (128, 2), (128, 1), (128, 2, "gather")]),
+                                         ("conv4", [(128, 2, "gather"), (128, 2, "grid")]),
+                                         ("conv5", [(256, 1, "gather"), (128, 2, "gather"), (256, 1, "grid")]),
+                                         ("conv6", [(64, 2), (128, 1), (256, 1), (256, 2, "gather")]),
+                                         ("conv7", [(256, 1, "grid"), (128, 2, "gather"), (256, 1, "gather")]),
                                          ("conv8", [(64, 4), (128, 2), (256, 1)])])
 def test_every_tile_same_bits(tdm, weights, patches, layer, tiles):
+    """Every tile and kernel form of a layer gives the same descriptor bits
+    (the gathered-row form skips the grid form's dropped rows, nothing else)."""
     net = tdm.Net(weights, precision="bf16")
     ref = net.forward(patches).cpu().numpy()
-    for nt, ms in tiles:
-        net.set_tile(layer, nt, ms)
-        assert np.array_equal(net.forward(patches).cpu().numpy(), ref), (layer, nt, ms)
+    for t in tiles:
+        net.set_tile(layer, *t)
+        if len(t) == 3:
+            assert net.forms()[layer] == t[2]
+        assert np.array_equal(net.forward(patches).cpu().numpy(), ref), (layer, t)
     with pytest.raises(tdm.TdmError):
         net.set_tile("conv2", 128, 1)  # conv2 has 64 outputs
+
+
+def test_fp8_gather_and_grid_forms_same_bits(tdm, weights, patches):
+    """E4M3 operands: the gathered-row and grid forms of conv3..conv7 agree bit for bit."""
+    net = tdm.Net(weights, precision="fp8")
+    net.calibrate(patches)
+    for layer in ("conv3", "conv4", "conv5", "conv6", "conv7"):
+        net.set_tile(layer, 128, 2, "grid")
+    ref = net.forward(patches).cpu().numpy()
+    for layer in ("conv3", "conv4", "conv5", "conv6", "conv7"):
+        net.set_tile(layer, 128, 2, "gather")
+    assert set(net.forms()[k] for k in ("conv3", "conv4", "conv5", "conv6", "conv7")) == {"gather"}
+    assert np.array_equal(net.forward(patches).cpu().numpy(), ref)
+    for layer in ("conv5", "conv6", "conv7"):
+        net.set_tile(layer, 256, 2, "gather")
+    assert np.array_equal(net.forward(patches).cpu().numpy(), ref)
+    tdm.device_status()
