@@ -135,6 +135,18 @@ __device__ __forceinline__ uint32_t pack_e4m3x4(float a, float b, float c, float
   return lo;
 }
 
+// 16 consecutive floats (16-byte aligned) as four vector loads.
+__device__ __forceinline__ void load16(const float* p, float (&v)[16]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float4 c = __ldg(reinterpret_cast<const float4*>(p) + k);
+    v[4 * k] = c.x;
+    v[4 * k + 1] = c.y;
+    v[4 * k + 2] = c.z;
+    v[4 * k + 3] = c.w;
+  }
+}
+
 // Persistent, warp-specialised implicit-GEMM convolution.  Each CTA walks the
 // tiles blockIdx.x, blockIdx.x + gridDim.x, ...; the load pipeline runs across
 // tile boundaries and the TMEM accumulator is double-buffered, so the epilogue
@@ -317,11 +329,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
           ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)(i * NT + c0), v);
           if (!valid) continue;
           const int n = n0 + c0;
+          float bs[16], sc[16];
+          load16(p.bias + n, bs);
+          if (FP8_IN) load16(p.wscale + n, sc);
 #pragma unroll
           for (int e = 0; e < 16; ++e) {
             float a = v[e];
-            if (FP8_IN) a = a * (p.in_scale * __ldg(p.wscale + n + e));
-            a += __ldg(p.bias + n + e);
+            if (FP8_IN) a = a * (p.in_scale * sc[e]);
+            a += bs[e];
             if (p.relu) a = fmaxf(a, 0.0f);
             v[e] = a;
           }
@@ -543,16 +558,27 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
         const int64_t b = row / Do3;
         const int tap = (int)(row - b * Do3);
 #pragma unroll 1
-        for (int c0 = 0; c0 < NT; c0 += 16) {
-          float v[16];
-          ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)(i * NT + c0), v);
+        for (int c1 = 0; c1 < NT; c1 += 32) {
+          uint32_t r2[2][16];  // 32 accumulator columns: two loads, one wait
+          const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)(i * NT + c1);
+          ptx::tmem_ld16_nowait(ta, r2[0]);
+          ptx::tmem_ld16_nowait(ta + 16, r2[1]);
+          ptx::tmem_wait_ld();
           if (!valid) continue;
-          const int n = n0 + c0;
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+          float v[16];
+#pragma unroll
+          for (int e = 0; e < 16; ++e) v[e] = __uint_as_float(r2[hh][e]);
+          const int n = n0 + c1 + 16 * hh;
+          float bs[16], sc[16];
+          load16(p.bias + n, bs);
+          if (FP8) load16(p.wscale + n, sc);
 #pragma unroll
           for (int e = 0; e < 16; ++e) {
             float a = v[e];
-            if (FP8) a = a * (p.in_scale * __ldg(p.wscale + n + e));
-            a += __ldg(p.bias + n + e);
+            if (FP8) a = a * (p.in_scale * sc[e]);
+            a += bs[e];
             if (p.relu) a = fmaxf(a, 0.0f);
             v[e] = a;
           }
@@ -578,6 +604,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
               o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
               *reinterpret_cast<uint4*>(p.out + (chunk0 + h) * p.out_cs + prow * 16) = o;
             }
+          }
           }
         }
       }
@@ -1045,32 +1072,38 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
     int sa = 0;
     uint32_t pha = 0;
     bool ok = true;
+    constexpr int kRowsPerThread = kC1Rows / (32 * kC1Prod);
     for (int64_t t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
+      // all 27 x 4 loads of this thread's rows in flight at once, issued
+      // before the wait for a free stage
+      float v[kRowsPerThread][27];
+#pragma unroll
+      for (int k = 0; k < kRowsPerThread; ++k) {
+        int64_t row = t * kC1Rows + pt + 32 * kC1Prod * k;
+        row = row < p.rows ? row : p.rows - 1;  // rows past the end load a valid row and store zeros
+        const int64_t b = row / 21952;
+        const int q = (int)(row - b * 21952);
+        const int z = q / 784, y = (q / 28) % 28, x = q % 28;
+        const float* src = p.patches + b * 27000 + z * 900 + y * 30 + x;
+#pragma unroll
+        for (int tp = 0; tp < 27; ++tp) v[k][tp] = __ldg(src + (tp / 9) * 900 + ((tp / 3) % 3) * 30 + (tp % 3));
+      }
       if (!wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
       uint8_t* st = sA + sa * kC1Stage;
-      for (int r = pt; r < kC1Rows; r += 32 * kC1Prod) {
-        const int64_t row = t * kC1Rows + r;
-        float v[32];
-        if (row < p.rows) {
-          const int64_t b = row / 21952;
-          const int q = (int)(row - b * 21952);
-          const int z = q / 784, y = (q / 28) % 28, x = q % 28;
-          const float* src = p.patches + b * 27000 + z * 900 + y * 30 + x;
 #pragma unroll
-          for (int tp = 0; tp < 27; ++tp) v[tp] = __ldg(src + (tp / 9) * 900 + ((tp / 3) % 3) * 30 + (tp % 3));
-        } else {
-#pragma unroll
-          for (int tp = 0; tp < 27; ++tp) v[tp] = 0.0f;
-        }
-#pragma unroll
-        for (int tp = 27; tp < 32; ++tp) v[tp] = 0.0f;
+      for (int k = 0; k < kRowsPerThread; ++k) {
+        const int r = pt + 32 * kC1Prod * k;
+        const float keep = t * kC1Rows + r < p.rows ? 1.0f : 0.0f;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
+          float f[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e) f[e] = 8 * j + e < 27 ? v[k][8 * j + e] * keep : 0.0f;
           uint4 o;
-          o.x = pack_bf16x2(v[8 * j + 0], v[8 * j + 1]);
-          o.y = pack_bf16x2(v[8 * j + 2], v[8 * j + 3]);
-          o.z = pack_bf16x2(v[8 * j + 4], v[8 * j + 5]);
-          o.w = pack_bf16x2(v[8 * j + 6], v[8 * j + 7]);
+          o.x = pack_bf16x2(f[0], f[1]);
+          o.y = pack_bf16x2(f[2], f[3]);
+          o.z = pack_bf16x2(f[4], f[5]);
+          o.w = pack_bf16x2(f[6], f[7]);
           *reinterpret_cast<uint4*>(st + ((size_t)j * kC1Rows + r) * 16) = o;
         }
       }
@@ -1114,6 +1147,14 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
   } else {
     // ---------------- epilogue: bias, ReLU, BF16 rows (conv2's chunk-planar input) ----------------
     const int q = warp & 3;
+    float bias[64];  // loaded once: every row of every tile adds the same 64 biases
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      float b16[16];
+      load16(p.bias + 16 * k, b16);
+#pragma unroll
+      for (int e = 0; e < 16; ++e) bias[16 * k + e] = b16[e];
+    }
     uint32_t j = 0;
     for (int64_t t = blockIdx.x; t < p.tiles; t += gridDim.x) {
       const uint32_t buf = j & 1u, use = j >> 1;
@@ -1125,22 +1166,23 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
       for (int i = 0; i < 4; ++i) {
         const int64_t row = t * kC1Rows + i * 128 + q * 32 + lane;
         const bool valid = row < p.rows;
-#pragma unroll 1
-        for (int c0 = 0; c0 < 64; c0 += 16) {
-          float v[16];
-          ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC + (uint32_t)(i * 64 + c0), v);
-          if (!valid) continue;
+        uint32_t r[4][16];  // the row's 64 accumulators: four loads, one wait
 #pragma unroll
-          for (int e = 0; e < 16; ++e) v[e] = fmaxf(v[e] + __ldg(p.bias + c0 + e), 0.0f);
+        for (int k = 0; k < 4; ++k)
+          ptx::tmem_ld16_nowait(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC + (uint32_t)(i * 64 + 16 * k), r[k]);
+        ptx::tmem_wait_ld();
+        if (!valid) continue;
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            uint4 o;
-            o.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
-            o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
-            o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
-            o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
-            *reinterpret_cast<uint4*>(p.out + (int64_t)(c0 / 8 + h) * p.out_cs + row * 16) = o;
-          }
+        for (int c = 0; c < 8; ++c) {
+          float f[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e) f[e] = fmaxf(__uint_as_float(r[c / 2][8 * (c % 2) + e]) + bias[8 * c + e], 0.0f);
+          uint4 o;
+          o.x = pack_bf16x2(f[0], f[1]);
+          o.y = pack_bf16x2(f[2], f[3]);
+          o.z = pack_bf16x2(f[4], f[5]);
+          o.w = pack_bf16x2(f[6], f[7]);
+          *reinterpret_cast<uint4*>(p.out + (int64_t)c * p.out_cs + row * 16) = o;
         }
       }
       ptx::tc_fence_before();

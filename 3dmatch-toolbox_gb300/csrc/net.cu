@@ -203,9 +203,9 @@ TcLayer make_tc_layer(int l, bool use_feat) {
     L.nt = 32;
     L.msub = 2;
   }
-  if (l >= 4 && l <= 6) {  // conv5..conv7: M over the valid output positions only
+  if (l >= 2 && l <= 6) {  // conv3..conv7: M over the valid output positions only
     L.gather = true;
-    L.nt = 256;
+    L.nt = L.cout == 128 ? 128 : 256;
     L.msub = 2;
   }
   return L;
