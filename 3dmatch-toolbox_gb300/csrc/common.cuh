@@ -213,6 +213,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;  // base offset 0, swizzle mode 0 (none)
 }
 
+// The start-address field is the descriptor's lowest 14 bits (address >> 4),
+// so the descriptor of an operand `bytes` further on (a multiple of 16, still
+// inside shared memory) is the same value plus bytes >> 4: MMA issue loops
+// build one base descriptor per operand and advance it with integer adds.
+__device__ __forceinline__ uint64_t desc_advance(uint64_t desc, uint32_t bytes) { return desc + (bytes >> 4); }
+
 // Instruction descriptor: FP32 accumulator, K-major A and B, M=128, N=n.
 // a_fmt/b_fmt: kind::f16 -> 0 F16, 1 BF16;  kind::f8f6f4 -> 0 E4M3, 1 E5M2.
 __host__ __device__ constexpr uint32_t make_idesc(uint32_t n, uint32_t m, uint32_t a_fmt, uint32_t b_fmt) {

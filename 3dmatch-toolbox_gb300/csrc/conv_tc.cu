@@ -247,6 +247,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
       uint32_t pha = 0, phb = 0;
       bool ok = true;
       const uint32_t lboA = (uint32_t)R * 16u;
+      const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), bDesc0 = ptx::smem_desc(sB_u, NT * 16, 128);
       uint32_t j = 0;  // tiles done by this CTA
       for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
         const int64_t m0 = (t / p.ntiles) * MCTA;
@@ -260,18 +261,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
           for (int cg = 0; cg < p.kgroups && ok; ++cg) {
             if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
             ptx::tc_fence_after();
-            const uint32_t aBase = sA_u + sa * a_stage;
+            const uint64_t aStage = ptx::desc_advance(aDesc0, sa * a_stage);
             for (int yx = 0; yx < p.nyx; ++yx) {
               if (!TDM_TIMED_WAIT(2, wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
               ptx::tc_fence_after();
-              const uint32_t bBase = sB_u + sb * b_stage;
+              const uint64_t bStage = ptx::desc_advance(bDesc0, sb * b_stage);
               const int off = (p.nyx > 1) ? (yx / 3) * p.D + (yx % 3) : 0;
+              const uint64_t aTap = ptx::desc_advance(aStage, (uint32_t)off * 16u);
+#pragma unroll 4
               for (int kk = 0; kk < p.cpg / 2; ++kk) {
-                const uint64_t bdesc = ptx::smem_desc(bBase + (2 * kk) * NT * 16, NT * 16, 128);
+                const uint64_t bdesc = ptx::desc_advance(bStage, (2 * kk) * NT * 16);
 #pragma unroll
                 for (int i = 0; i < MSUB; ++i) {
-                  const uint64_t adesc =
-                      ptx::smem_desc(aBase + (2 * kk) * lboA + (uint32_t)(i * 128 + off) * 16u, lboA, 128);
+                  const uint64_t adesc = ptx::desc_advance(aTap, (2 * kk) * lboA + (uint32_t)(i * 128) * 16u);
                   if (FP8_IN) ptx::mma_f8(dbase + i * NT, adesc, bdesc, idesc, accumulate);
                   else ptx::mma_f16(dbase + i * NT, adesc, bdesc, idesc, accumulate);
                 }
@@ -498,6 +500,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
       // ---------------- MMA issuer ----------------
       constexpr uint32_t idesc = FP8 ? ptx::make_idesc(NT, 128, 0, 0) : ptx::make_idesc(NT, 128, 1, 1);
       constexpr uint32_t lboA = MCTA * 16u;
+      const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), bDesc0 = ptx::smem_desc(sB_u, NT * 16, 128);
       int sa = 0, sb = 0;
       uint32_t pha = 0, phb = 0;
       bool ok = true;
@@ -517,12 +520,14 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
                 break;
               }
               ptx::tc_fence_after();
-              const uint32_t aBase = sA_u + sa * a_stage, bBase = sB_u + sb * b_stage;
+              const uint64_t aStage = ptx::desc_advance(aDesc0, sa * a_stage);
+              const uint64_t bStage = ptx::desc_advance(bDesc0, sb * b_stage);
+#pragma unroll 4
               for (int kk = 0; kk < cpg / 2; ++kk) {
-                const uint64_t bdesc = ptx::smem_desc(bBase + (2 * kk) * NT * 16, NT * 16, 128);
+                const uint64_t bdesc = ptx::desc_advance(bStage, (2 * kk) * NT * 16);
 #pragma unroll
                 for (int i = 0; i < MSUB; ++i) {
-                  const uint64_t adesc = ptx::smem_desc(aBase + (2 * kk) * lboA + (uint32_t)(i * 128) * 16u, lboA, 128);
+                  const uint64_t adesc = ptx::desc_advance(aStage, (2 * kk) * lboA + (uint32_t)(i * 128) * 16u);
                   if (FP8) ptx::mma_f8(dbase + i * NT, adesc, bdesc, idesc, accumulate);
                   else ptx::mma_f16(dbase + i * NT, adesc, bdesc, idesc, accumulate);
                 }
@@ -801,6 +806,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
       // ---------------- MMA issuer ----------------
       constexpr uint32_t idesc = ptx::make_idesc(kDxfN, 128, 1, 1);
       const uint32_t lboA = (uint32_t)R * 16u;
+      const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), wDesc0 = ptx::smem_desc(sW_u, kDxfN * 16, 128);
       int sa = 0;
       uint32_t pha = 0;
 #ifdef TDM_WAIT_STATS
@@ -819,19 +825,21 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
         for (int zt = 0; zt < 3 && ok; ++zt) {
           if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
           ptx::tc_fence_after();
-          const uint32_t aBase = sA_u + sa * a_stage;
+          // one thread issues every MMA: descriptors are advanced by adds, not rebuilt
+          const uint64_t aStage = ptx::desc_advance(aDesc0, sa * a_stage);
+#pragma unroll
           for (int dy = 0; dy < 3; ++dy) {
-            const uint32_t wBase = sW_u + (zt * 3 + dy) * kDxfBlock;
+            const uint64_t aRow = ptx::desc_advance(aStage, (uint32_t)(dy * p.D) * 16u);
+            const uint64_t wDesc = ptx::desc_advance(wDesc0, (uint32_t)(zt * 3 + dy) * kDxfBlock);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
-              const uint64_t bdesc = ptx::smem_desc(wBase + (2 * kk) * kDxfN * 16, kDxfN * 16, 128);
+              const uint64_t bdesc = ptx::desc_advance(wDesc, (2 * kk) * kDxfN * 16);
 #pragma unroll
               for (int i = 0; i < MSUB; ++i) {
-                const uint64_t adesc =
-                    ptx::smem_desc(aBase + (2 * kk) * lboA + (uint32_t)(i * kDxfSub + dy * p.D) * 16u, lboA, 128);
+                const uint64_t adesc = ptx::desc_advance(aRow, (2 * kk) * lboA + (uint32_t)(i * kDxfSub) * 16u);
                 ptx::mma_f16(dbase + i * kDxfN, adesc, bdesc, idesc, accumulate);
               }
-              accumulate = 1;
+              accumulate = 1;  // each sub-tile's first MMA (zt = dy = kk = 0) starts its accumulator
             }
           }
           ptx::mma_commit(emptyA + 8 * sa);
@@ -1117,6 +1125,7 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
       // ---------------- MMA issuer ----------------
       constexpr uint32_t idesc = ptx::make_idesc(64, 128, 1, 1);
       constexpr uint32_t lboA = kC1Rows * 16u;
+      const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), wDesc0 = ptx::smem_desc(sW_u, 64 * 16, 128);
       int sa = 0;
       uint32_t pha = 0;
       bool ok = wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_MMA);
@@ -1126,13 +1135,14 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
         if (!wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
         if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
         ptx::tc_fence_after();
-        const uint32_t aBase = sA_u + sa * kC1Stage, dbase = tmem + buf * ACC;
+        const uint32_t dbase = tmem + buf * ACC;
+        const uint64_t aStage = ptx::desc_advance(aDesc0, sa * kC1Stage);
 #pragma unroll
         for (int kk = 0; kk < 2; ++kk) {
-          const uint64_t bdesc = ptx::smem_desc(sW_u + (2 * kk) * 64 * 16, 64 * 16, 128);
+          const uint64_t bdesc = ptx::desc_advance(wDesc0, (2 * kk) * 64 * 16);
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
-            const uint64_t adesc = ptx::smem_desc(aBase + (2 * kk) * lboA + (uint32_t)(i * 128) * 16u, lboA, 128);
+            const uint64_t adesc = ptx::desc_advance(aStage, (2 * kk) * lboA + (uint32_t)(i * 128) * 16u);
             ptx::mma_f16(dbase + i * 64, adesc, bdesc, idesc, kk > 0 ? 1u : 0u);
           }
         }
@@ -1200,7 +1210,7 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
 }
 
 int slab_rows(const TcLayer& L) {
-  if (L.dxf) return (L.msub - 1) * kDxfSub + 128 + 2 * L.D;  // exact: three stages must fit beside the weights
+  if (L.dxf) return (L.msub - 1) * kDxfSub + 128 + 2 * L.D;  // exact: the stages must fit beside the weights
   int r = L.msub * 128 + (L.nyx > 1 ? 2 * L.D + 2 : 0);
   return (r + 7) & ~7;
 }

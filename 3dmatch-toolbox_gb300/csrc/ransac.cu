@@ -89,6 +89,7 @@ __device__ bool trial_model(const float* x, const float* y, int m, uint64_t seed
 __global__ __launch_bounds__(256) void trials_kernel(const float* __restrict__ x, const float* __restrict__ y,
                                                      const int32_t* __restrict__ m_dev, int m_max, int smem_pts,
                                                      uint64_t seed, int iters, float thr, int32_t* __restrict__ counts,
+                                                     float* __restrict__ models,
                                                      unsigned long long* __restrict__ best) {
   extern __shared__ float sp[];
   int m = *m_dev;
@@ -109,6 +110,11 @@ __global__ __launch_bounds__(256) void trials_kernel(const float* __restrict__ x
     const float* ys = staged ? sp + 3 * smem_pts : y;
     float Rf[9], tf[3];
     if (trial_model(xs, ys, m, seed, (uint32_t)h, Rf, tf)) {
+      // kept for the winner: the finalize step reads it instead of refitting
+      float4* mo = reinterpret_cast<float4*>(models + 12 * (int64_t)h);
+      mo[0] = make_float4(Rf[0], Rf[1], Rf[2], Rf[3]);
+      mo[1] = make_float4(Rf[4], Rf[5], Rf[6], Rf[7]);
+      mo[2] = make_float4(Rf[8], tf[0], tf[1], tf[2]);
       const float thr2 = thr * thr;
       for (int i = 0; i < m; ++i) c += is_inlier(xs + 3 * i, ys + 3 * i, Rf, tf, thr2) ? 1 : 0;
     }
@@ -122,6 +128,7 @@ __global__ __launch_bounds__(1024) void finalize_kernel(const float* __restrict_
                                                         const int32_t* __restrict__ m_dev, int m_max, uint64_t seed,
                                                         int iters, float thr, int adaptive, int max_trials,
                                                         const int32_t* __restrict__ counts,
+                                                        const float* __restrict__ models,
                                                         const unsigned long long* __restrict__ best,
                                                         double* __restrict__ rt, int32_t* __restrict__ inliers,
                                                         int32_t* __restrict__ info) {
@@ -161,13 +168,10 @@ __global__ __launch_bounds__(1024) void finalize_kernel(const float* __restrict_
     s_h = h;
     s_trials = trials;
     s_ok = 0;
-    if (h >= 0 && counts[h] > 0) {
-      float Rf[9], tf[3];
-      if (trial_model(x, y, m, seed, (uint32_t)h, Rf, tf)) {
-        for (int i = 0; i < 9; ++i) sR[i] = Rf[i];
-        for (int i = 0; i < 3; ++i) st[i] = tf[i];
-        s_ok = 1;
-      }
+    if (h >= 0 && counts[h] > 0) {  // a positive count implies a valid trial model, stored by trials_kernel
+      for (int i = 0; i < 9; ++i) sR[i] = models[12 * (int64_t)h + i];
+      for (int i = 0; i < 3; ++i) st[i] = models[12 * (int64_t)h + 9 + i];
+      s_ok = 1;
     }
     s_base = 0;
   }
@@ -239,10 +243,13 @@ cudaError_t trials_smem_cap() {
 
 using namespace tdm;
 
+// Workspace: best-trial word, one inlier count and one FP32 model (R, t:
+// 12 floats) per trial.
 extern "C" size_t tdm_ransac_workspace_bytes(int32_t m_max, int32_t iterations) {
   (void)m_max;
   if (iterations < 0) return 0;
-  return align256(8) + align256((size_t)(iterations > 0 ? iterations : 1) * 4);
+  const size_t n = (size_t)(iterations > 0 ? iterations : 1);
+  return align256(8) + align256(n * 4) + n * 48;
 }
 
 extern "C" tdm_status tdm_ransac(const float* x, const float* y, const int32_t* m_dev, int32_t m_max,
@@ -254,6 +261,7 @@ extern "C" tdm_status tdm_ransac(const float* x, const float* y, const int32_t* 
   uint8_t* w = static_cast<uint8_t*>(ws);
   unsigned long long* best = reinterpret_cast<unsigned long long*>(w);
   int32_t* counts = reinterpret_cast<int32_t*>(w + align256(8));
+  float* models = reinterpret_cast<float*>(w + align256(8) + align256((size_t)(prm->iterations > 0 ? prm->iterations : 1) * 4));
   TDM_CHECK_CUDA(cudaMemsetAsync(best, 0, 8, s));
   const int iters = prm->iterations;
   if (iters > 0) {
@@ -261,11 +269,11 @@ extern "C" tdm_status tdm_ransac(const float* x, const float* y, const int32_t* 
     size_t smem = (size_t)6 * smem_pts * sizeof(float);
     TDM_CHECK_CUDA(trials_smem_cap());
     trials_kernel<<<(iters + 255) / 256, 256, smem, s>>>(x, y, m_dev, m_max, smem_pts, prm->seed, iters,
-                                                          prm->threshold, counts, best);
+                                                          prm->threshold, counts, models, best);
     TDM_CHECK_LAUNCH("trials_kernel");
   }
   finalize_kernel<<<1, 1024, 0, s>>>(x, y, m_dev, m_max, prm->seed, iters, prm->threshold, prm->adaptive ? 1 : 0,
-                                     prm->max_trials, counts, best, rt, inliers, info);
+                                     prm->max_trials, counts, models, best, rt, inliers, info);
   TDM_CHECK_LAUNCH("finalize_kernel");
   return TDM_OK;
 }
@@ -290,7 +298,7 @@ extern "C" tdm_status tdm_pairs_to_points(const float* ka, const float* kb, cons
 // only pointers it was given), and serving loops that forbid cudaMalloc after
 // start-up because it synchronizes the device and can fail under a memory
 // budget.  For them this variant keeps its scratch in a fixed device array of
-// this file, sized for kNoAllocMaxTrials trials (about 512 KB, held by every
+// this file, sized for kNoAllocMaxTrials trials (about 6.8 MB, held by every
 // GPU that loads the library until the process exits).
 //
 // The array is shared by every call: the best-trial word is cleared at the
@@ -304,7 +312,8 @@ namespace {
 
 constexpr int kNoAllocMaxTrials = 131072;
 constexpr size_t kNoAllocCountsOffset = 256;  // best word, padded; then counts
-static __device__ __align__(256) unsigned char g_ransac_scratch[kNoAllocCountsOffset + 4 * (size_t)kNoAllocMaxTrials];
+constexpr size_t kNoAllocModelsOffset = kNoAllocCountsOffset + 4 * (size_t)kNoAllocMaxTrials;  // then 12 floats per trial
+static __device__ __align__(256) unsigned char g_ransac_scratch[kNoAllocModelsOffset + 48 * (size_t)kNoAllocMaxTrials];
 
 // Device address of g_ransac_scratch, resolved once per device with that
 // device current (the host-side symbol is only a stand-in, never a device
@@ -345,6 +354,7 @@ extern "C" tdm_status tdm_ransac_noalloc(const float* x, const float* y, const i
   uint8_t* w = static_cast<uint8_t*>(scratch);
   unsigned long long* best = reinterpret_cast<unsigned long long*>(w);
   int32_t* counts = reinterpret_cast<int32_t*>(w + kNoAllocCountsOffset);
+  float* models = reinterpret_cast<float*>(w + kNoAllocModelsOffset);
   TDM_CHECK_CUDA(cudaMemsetAsync(best, 0, 8, s));  // the best word must start at zero
   const int iters = prm->iterations;
   if (iters > 0) {
@@ -352,11 +362,11 @@ extern "C" tdm_status tdm_ransac_noalloc(const float* x, const float* y, const i
     size_t smem = (size_t)6 * smem_pts * sizeof(float);
     TDM_CHECK_CUDA(trials_smem_cap());
     trials_kernel<<<(iters + 255) / 256, 256, smem, s>>>(x, y, m_dev, m_max, smem_pts, prm->seed, iters,
-                                                          prm->threshold, counts, best);
+                                                          prm->threshold, counts, models, best);
     TDM_CHECK_LAUNCH("trials_kernel (noalloc)");
   }
   finalize_kernel<<<1, 1024, 0, s>>>(x, y, m_dev, m_max, prm->seed, iters, prm->threshold, prm->adaptive ? 1 : 0,
-                                     prm->max_trials, counts, best, rt, inliers, info);
+                                     prm->max_trials, counts, models, best, rt, inliers, info);
   TDM_CHECK_LAUNCH("finalize_kernel (noalloc)");
   return TDM_OK;
 }

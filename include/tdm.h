@@ -192,7 +192,8 @@ typedef struct tdm_ransac_params {
  * m_dev (device int32) so the call needs no host round trip.  rt_dev: 12
  * doubles (3x4 row-major, FP64 Kabsch refit on the winner's inliers);
  * inliers_dev: m_max int32; info_dev: 4 int32 = {n_inliers, best_trial,
- * best_count, trials_run}. */
+ * best_count, trials_run}.  Workspace: the best-trial word, then per trial its
+ * inlier count and FP32 model. */
 size_t tdm_ransac_workspace_bytes(int32_t m_max, int32_t iterations);
 tdm_status tdm_ransac(const float* x_dev, const float* y_dev, const int32_t* m_dev, int32_t m_max,
                       const tdm_ransac_params* params, double* rt_dev, int32_t* inliers_dev, int32_t* info_dev,
@@ -201,7 +202,7 @@ tdm_status tdm_ransac(const float* x_dev, const float* y_dev, const int32_t* m_d
  * RANSAC is MATLAB).  For callers that cannot allocate device memory -- a
  * foreign-function binding holding no device allocator, or a serving loop that
  * forbids cudaMalloc after start-up -- the per-trial scratch lives in a fixed
- * device array inside the library (about 512 KB per GPU that loads it, kept
+ * device array inside the library (about 6.8 MB per GPU that loads it, kept
  * until the process exits).  Limit: params->iterations <= 131072 trials;
  * larger values return TDM_ERR_INVALID_ARG.  The call allocates nothing.  Its
  * first call on a device looks up the array's device address, so make that
