@@ -4,8 +4,9 @@
 // (core/external/peter/ransac.m:113-232) and estimateRt.m.  Model x = R y + t
 // (x: fragment-1 keypoints, y: fragment-2 keypoints).  Every trial h draws 3
 // distinct correspondences from a counter-based stream (splitmix64 keyed by
-// seed and 3h+j), fits R,t with Kabsch in FP64 (covariance, SVD through the
-// Jacobi eigen-decomposition of H^T H), and counts inliers in FP32 with the
+// seed and 3h+j), fits R,t with Kabsch in FP32 (covariance, SVD through the
+// Jacobi eigen-decomposition of H^T H; the model is used in FP32 for the
+// inlier tests, and FP32 issues far faster than FP64), and counts inliers with the
 // strict |x - (R y + t)| < threshold of euc3Ddist.  The best count wins and
 // ties go to the later trial (ransac.m:194 uses >=).  The final model is the
 // FP64 Kabsch refit on the winner's inliers (ransacfitRt.m:37).
@@ -73,16 +74,12 @@ __device__ __forceinline__ bool is_inlier(const float* xi, const float* yi, cons
   return d2 < thr2;
 }
 
-// Trial model for h (false when the sample is degenerate).
+// Trial model for h, fitted in FP32 (false when the sample is degenerate).
 __device__ bool trial_model(const float* x, const float* y, int m, uint64_t seed, uint32_t h, float Rf[9],
                             float tf[3]) {
   int s[3];
   sample3(seed, h, m, s);
-  double R[9], t[3];
-  if (!kabsch(x, y, s, 3, R, t)) return false;
-  for (int i = 0; i < 9; ++i) Rf[i] = (float)R[i];
-  for (int i = 0; i < 3; ++i) tf[i] = (float)t[i];
-  return true;
+  return kabsch3f(x, y, s, Rf, tf);
 }
 
 // One thread per trial; correspondences staged in shared memory (x then y).
