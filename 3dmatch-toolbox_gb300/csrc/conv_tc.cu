@@ -414,8 +414,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
 // ---------------------------------------------------------------------------
 constexpr int kGWarps = 4;                          // gather warps (warps 6..9)
 constexpr int kGThreads = kThreads + 32 * kGWarps;
-constexpr int kGNSA = 4;                            // A stages
-constexpr int kGDepth = 3;                          // stages a gather thread keeps in flight
+constexpr int kGNSA = 4;                            // A stages (gathered rows)
+constexpr int kXNSA = 3;                            // A stages (x runs: three B stages per A stage)
 
 // 16-byte global -> shared copy; src_bytes = 0 writes zeros without reading.
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
@@ -427,7 +427,7 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-template <int NT, int MSUB, bool FP8>
+template <int NT, int MSUB, bool FP8, bool XRUN>
 __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KParams p) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr int MCTA = MSUB * 128;
@@ -436,21 +436,24 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
   constexpr uint32_t TMEM_COLS = tmem_cols_for(NBUF * ACC_COLS);
   static_assert(ACC_COLS <= 512, "the accumulator must fit in TMEM");
   constexpr int E = FP8 ? 16 : 8;  // channels per 16-byte chunk
+  constexpr int NSA = XRUN ? kXNSA : kGNSA;  // A stages
+  constexpr int DEPTH = NSA - 1;              // stages a gather thread keeps in flight
+  constexpr int RS = MCTA + (XRUN ? 8 : 0);   // rows per A stage (x-run form: +2 for the dx shifts, padded)
   const int nsb = p.nsb, cpg = p.cpg;
-  const uint32_t a_stage = 16u * (uint32_t)cpg * MCTA;
+  const uint32_t a_stage = 16u * (uint32_t)cpg * RS;
   constexpr uint32_t b_stage = NT * 128u;
-  uint8_t* sB = smem + kGNSA * a_stage;
+  uint8_t* sB = smem + NSA * a_stage;
   uint64_t* bars = reinterpret_cast<uint64_t*>(sB + (size_t)nsb * b_stage);
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * kGNSA + 2 * MAX_NSB + 5);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * NSA + 2 * MAX_NSB + 5);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (!__syncthreads_and(aborted(p.err) ? 0 : 1)) return;  // another CTA already failed
 
-  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * kGNSA;
-  const uint32_t fullB = emptyA + 8 * kGNSA, emptyB = fullB + 8 * MAX_NSB;
+  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * NSA;
+  const uint32_t fullB = emptyA + 8 * NSA, emptyB = fullB + 8 * MAX_NSB;
   const uint32_t accFull = emptyB + 8 * MAX_NSB, accEmpty = accFull + 16, done = accEmpty + 16;
   if (threadIdx.x == 0) {
-    for (int i = 0; i < kGNSA; ++i) {
+    for (int i = 0; i < NSA; ++i) {
       ptx::mbar_init(fullA + 8 * i, 32 * kGWarps);  // every gather thread arrives
       ptx::mbar_init(emptyA + 8 * i, 1);
     }
@@ -470,6 +473,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
   const uint32_t tmem = *tmem_holder;
   const uint32_t sA_u = ptx::smem_u32(smem), sB_u = ptx::smem_u32(sB);
   const int Do2 = p.Do * p.Do, Do3 = Do2 * p.Do;
+  const int Dx = XRUN ? p.D : p.Do;  // x extent of the M rows
 
   if (warp == 0) {
     if (lane == 0) {
@@ -499,7 +503,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
       constexpr uint32_t idesc = FP8 ? ptx::make_idesc(NT, 128, 0, 0) : ptx::make_idesc(NT, 128, 1, 1);
-      constexpr uint32_t lboA = MCTA * 16u;
+      constexpr uint32_t lboA = RS * 16u;
       const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), bDesc0 = ptx::smem_desc(sB_u, NT * 16, 128);
       int sa = 0, sb = 0;
       uint32_t pha = 0, phb = 0;
@@ -511,32 +515,35 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
         ptx::tc_fence_after();
         const uint32_t dbase = tmem + buf * ACC_COLS;
         uint32_t accumulate = 0;
+        // A stage per (dz, K group, tap) -- or per (dz, K group, dy) in the
+        // x-run form, where the three dx taps read it shifted by dx rows
+        constexpr int TAPS_PER_A = XRUN ? 3 : 1;
         for (int zt = 0; zt < p.nz && ok; ++zt)
           for (int cg = 0; cg < p.kgroups && ok; ++cg)
-            for (int yx = 0; yx < p.nyx; ++yx) {
-              if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA) ||
-                  !wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA)) {
-                ok = false;
-                break;
-              }
-              ptx::tc_fence_after();
+            for (int ya = 0; ya < p.nyx / TAPS_PER_A && ok; ++ya) {
+              if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
               const uint64_t aStage = ptx::desc_advance(aDesc0, sa * a_stage);
-              const uint64_t bStage = ptx::desc_advance(bDesc0, sb * b_stage);
+              for (int dx = 0; dx < TAPS_PER_A; ++dx) {
+                if (!wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+                ptx::tc_fence_after();
+                const uint64_t bStage = ptx::desc_advance(bDesc0, sb * b_stage);
+                const uint64_t aTap = ptx::desc_advance(aStage, (uint32_t)dx * 16u);
 #pragma unroll 4
-              for (int kk = 0; kk < cpg / 2; ++kk) {
-                const uint64_t bdesc = ptx::desc_advance(bStage, (2 * kk) * NT * 16);
+                for (int kk = 0; kk < cpg / 2; ++kk) {
+                  const uint64_t bdesc = ptx::desc_advance(bStage, (2 * kk) * NT * 16);
 #pragma unroll
-                for (int i = 0; i < MSUB; ++i) {
-                  const uint64_t adesc = ptx::desc_advance(aStage, (2 * kk) * lboA + (uint32_t)(i * 128) * 16u);
-                  if (FP8) ptx::mma_f8(dbase + i * NT, adesc, bdesc, idesc, accumulate);
-                  else ptx::mma_f16(dbase + i * NT, adesc, bdesc, idesc, accumulate);
+                  for (int i = 0; i < MSUB; ++i) {
+                    const uint64_t adesc = ptx::desc_advance(aTap, (2 * kk) * lboA + (uint32_t)(i * 128) * 16u);
+                    if (FP8) ptx::mma_f8(dbase + i * NT, adesc, bdesc, idesc, accumulate);
+                    else ptx::mma_f16(dbase + i * NT, adesc, bdesc, idesc, accumulate);
+                  }
+                  accumulate = 1;
                 }
-                accumulate = 1;
+                ptx::mma_commit(emptyB + 8 * sb);
+                if (++sb == nsb) { sb = 0; phb ^= 1; }
               }
-              ptx::mma_commit(emptyB + 8 * sb);
-              if (++sb == nsb) { sb = 0; phb ^= 1; }
               ptx::mma_commit(emptyA + 8 * sa);
-              if (++sa == kGNSA) { sa = 0; pha ^= 1; }
+              if (++sa == NSA) { sa = 0; pha ^= 1; }
             }
         ptx::mma_commit(accFull + 8 * buf);  // fires when this tile's MMAs are complete
         ++j;
@@ -559,9 +566,20 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
 #pragma unroll 1
       for (int i = 0; i < MSUB; ++i) {
         const int64_t row = m0 + i * 128 + q * 32 + lane;
-        const bool valid = row < p.rows;
-        const int64_t b = row / Do3;
-        const int tap = (int)(row - b * Do3);
+        bool valid = row < p.rows;
+        int64_t b, pos;  // patch, output position (row of the next layer's grid)
+        int tap;         // output position within the patch
+        if (XRUN) {      // rows (b, z, y, x < D): outputs where x < Do
+          const int64_t yz = row / Dx;
+          const int x = (int)(row - yz * Dx);
+          valid = valid && x < p.Do;
+          b = yz / Do2;
+          tap = (int)(yz - b * Do2) * p.Do + x;
+        } else {
+          b = row / Do3;
+          tap = (int)(row - b * Do3);
+        }
+        pos = b * Do3 + tap;
 #pragma unroll 1
         for (int c1 = 0; c1 < NT; c1 += 32) {
           uint32_t r2[2][16];  // 32 accumulator columns: two loads, one wait
@@ -591,7 +609,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
           // conv8's operand (chunk = tap * Cout/E + channel chunk, row = patch)
           const bool taps = p.out_mode == TC_OUT_C8_TAPS;
           const int64_t chunk0 = (taps ? (int64_t)tap * (p.cout / E) : 0) + n / E;
-          const int64_t prow = taps ? b : row;
+          const int64_t prow = taps ? b : pos;
           if (FP8) {
             uint4 o;
             o.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
@@ -623,58 +641,68 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
     const int gt = threadIdx.x - kThreads;  // 0 .. 127: row gt of every 128-row sub-tile
     int sa = 0;
     uint32_t pha = 0;
-    int pend[kGDepth];  // stages copied but not yet published, oldest first from q0
+    int pend[DEPTH];  // stages copied but not yet published, oldest first from q0
     int q0 = 0, np = 0;
     bool ok = true;
     const int64_t plane = (int64_t)p.D * p.D;
     for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
       const int64_t m0 = (t / p.ntiles) * MCTA;
-      int64_t base[MSUB];
-      uint32_t bytes[MSUB];
+      // this thread's stage rows: gt + 128 i, and in the x-run form also the
+      // padding row MCTA + gt (gt < 8; the first rows of the next tile)
+      constexpr int NR = MSUB + (XRUN ? 1 : 0);
+      int64_t base[NR];
+      uint32_t bytes[NR];
+      int slot[NR];
 #pragma unroll
-      for (int i = 0; i < MSUB; ++i) {
-        const int64_t row = m0 + i * 128 + gt;
+      for (int i = 0; i < NR; ++i) {
+        slot[i] = i < MSUB ? i * 128 + gt : MCTA + gt;
+        const int64_t row = m0 + slot[i];
         base[i] = 0;
         bytes[i] = 0;  // rows past the end are zero-filled
-        if (row < p.rows) {
-          const int64_t b = row / Do3;
-          const int r = (int)(row - b * Do3);
-          const int z = r / Do2, y = (r / p.Do) % p.Do, x = r % p.Do;
-          base[i] = ((b * p.D + z) * p.D + y) * p.D + x;
+        if (row < p.rows && (i < MSUB || gt < 8)) {
+          const int64_t yz = row / Dx;  // (b, z, y)
+          const int x = (int)(row - yz * Dx);
+          const int64_t b = yz / Do2;
+          const int r = (int)(yz - b * Do2);
+          base[i] = ((b * p.D + r / p.Do) * p.D + r % p.Do) * p.D + x;
           bytes[i] = 16;
         }
       }
+      constexpr int TAPS_PER_A = XRUN ? 3 : 1;
       for (int zt = 0; zt < p.nz && ok; ++zt)
         for (int cg = 0; cg < p.kgroups && ok; ++cg)
-          for (int yx = 0; yx < p.nyx; ++yx) {
+          for (int ya = 0; ya < p.nyx / TAPS_PER_A; ++ya) {
             if (!wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
-            const int64_t off = zt * plane + (yx / 3) * p.D + (yx % 3);
-            const uint32_t dst = sA_u + sa * a_stage + gt * 16;
+            // tap offset in the input grid (the x-run form stages dx = 0; dx
+            // comes from the MMA's row shift)
+            const int64_t off = XRUN ? zt * plane + ya * p.D : zt * plane + (ya / 3) * p.D + (ya % 3);
+            const uint32_t dst = sA_u + sa * a_stage;
             const uint8_t* cbase = p.act + (int64_t)cg * cpg * p.act_cs;
 #pragma unroll
-            for (int i = 0; i < MSUB; ++i) {
+            for (int i = 0; i < NR; ++i) {
+              if (i == MSUB && gt >= 8) continue;
               const uint8_t* src = cbase + (base[i] + off) * 16;
 #pragma unroll 4
               for (int c = 0; c < cpg; ++c)
-                cp_async16(dst + (uint32_t)(c * MCTA + i * 128) * 16u, src + c * p.act_cs, bytes[i]);
+                cp_async16(dst + (uint32_t)(c * RS + slot[i]) * 16u, src + c * p.act_cs, bytes[i]);
             }
             cp_async_commit();
-            pend[(q0 + np) % kGDepth] = sa;
-            if (++np == kGDepth) {  // publish the oldest stage once its copies have landed
-              cp_async_wait<kGDepth - 1>();
+            pend[(q0 + np) % DEPTH] = sa;
+            if (++np == DEPTH) {  // publish the oldest stage once its copies have landed
+              cp_async_wait<DEPTH - 1>();
               ptx::fence_proxy_async_smem();  // generic-proxy writes visible to the tensor core
               mbar_arrive(fullA + 8 * pend[q0]);
-              q0 = (q0 + 1) % kGDepth;
+              q0 = (q0 + 1) % DEPTH;
               --np;
             }
-            if (++sa == kGNSA) { sa = 0; pha ^= 1; }
+            if (++sa == NSA) { sa = 0; pha ^= 1; }
           }
     }
     cp_async_wait<0>();  // no copy may still be in flight when the CTA exits
     ptx::fence_proxy_async_smem();
     for (; np > 0; --np) {
       mbar_arrive(fullA + 8 * pend[q0]);
-      q0 = (q0 + 1) % kGDepth;
+      q0 = (q0 + 1) % DEPTH;
     }
   }
   ptx::tc_fence_before();
@@ -1225,10 +1253,13 @@ int chunks_per_group(const TcLayer& L) {
 size_t a_stage_bytes(const TcLayer& L) { return (size_t)16 * chunks_per_group(L) * slab_rows(L); }
 
 // gathered-row form: one (tap, K group) of msub*128 rows per A stage
-size_t gather_stage_bytes(const TcLayer& L) { return (size_t)16 * chunks_per_group(L) * L.msub * 128; }
+size_t gather_stage_bytes(const TcLayer& L) {
+  return (size_t)16 * chunks_per_group(L) * (L.msub * 128 + (L.xrun ? 8 : 0));
+}
+int gather_stages(const TcLayer& L) { return L.xrun ? kXNSA : kGNSA; }
 
 int weight_stages(const TcLayer& L) {
-  const size_t a = L.gather ? kGNSA * gather_stage_bytes(L) : NSA * a_stage_bytes(L);
+  const size_t a = L.gather ? gather_stages(L) * gather_stage_bytes(L) : NSA * a_stage_bytes(L);
   if (a + kSmemReserve >= kSmemLimit) return 0;
   size_t left = kSmemLimit - kSmemReserve - a;
   int n = (int)(left / ((size_t)L.nt * 128));
@@ -1237,7 +1268,7 @@ int weight_stages(const TcLayer& L) {
 
 size_t smem_bytes(const TcLayer& L) {
   if (L.dxf) return kDxfWBytes + kDxfNSA * a_stage_bytes(L) + kDxfXchg + kDxfStage + 32 + kSmemReserve;
-  if (L.gather) return kGNSA * gather_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
+  if (L.gather) return gather_stages(L) * gather_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
   return NSA * a_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
 }
 
@@ -1271,9 +1302,9 @@ tdm_status launch_t(const KParams& kp, size_t smem, cudaStream_t s) {
   return TDM_OK;
 }
 
-template <int NT, int MSUB, bool FP8>
+template <int NT, int MSUB, bool FP8, bool XRUN>
 tdm_status launch_g(const KParams& kp, size_t smem, cudaStream_t s) {
-  auto kern = tc_conv_gather_kernel<NT, MSUB, FP8>;
+  auto kern = tc_conv_gather_kernel<NT, MSUB, FP8, XRUN>;
   size_t req = std::max<size_t>(smem, 120 * 1024);
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
@@ -1414,7 +1445,8 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
                 "tc layer: operands must be 16-byte aligned");
     const int64_t D3 = (int64_t)L.D * L.D * L.D;
     TDM_REQUIRE(a.rows % D3 == 0, "tc layer: input rows must be whole patches");
-    kp.rows = a.rows / D3 * L.Do * L.Do * L.Do;  // M = valid output positions
+    // M = valid output positions, or in the x-run form whole x runs of them
+    kp.rows = a.rows / D3 * L.Do * L.Do * (L.xrun ? L.D : L.Do);
     if (kp.rows == 0) return TDM_OK;
     kp.nsb = weight_stages(L);
     const int64_t mcta = (int64_t)L.msub * 128;
@@ -1422,9 +1454,16 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
     kp.total_tiles = ((kp.rows + mcta - 1) / mcta) * kp.ntiles;
     const size_t smem = smem_bytes(L);
     const bool f8 = L.fp8_in;
-    if (L.nt == 256 && L.msub == 2) return f8 ? launch_g<256, 2, true>(kp, smem, s) : launch_g<256, 2, false>(kp, smem, s);
-    if (L.nt == 256 && L.msub == 1) return f8 ? launch_g<256, 1, true>(kp, smem, s) : launch_g<256, 1, false>(kp, smem, s);
-    return f8 ? launch_g<128, 2, true>(kp, smem, s) : launch_g<128, 2, false>(kp, smem, s);
+#define TDM_G_CASE(NT_, MS_)                                                              \
+  if (L.nt == NT_ && L.msub == MS_) {                                                     \
+    if (L.xrun) return f8 ? launch_g<NT_, MS_, true, true>(kp, smem, s) : launch_g<NT_, MS_, false, true>(kp, smem, s); \
+    return f8 ? launch_g<NT_, MS_, true, false>(kp, smem, s) : launch_g<NT_, MS_, false, false>(kp, smem, s);           \
+  }
+    TDM_G_CASE(256, 2)
+    TDM_G_CASE(256, 1)
+    TDM_G_CASE(128, 2)
+#undef TDM_G_CASE
+    return fail(TDM_ERR_UNSUPPORTED, "tc layer: unsupported gathered-row tile");
   }
   kp.nsb = weight_stages(L);
   TDM_REQUIRE(kp.nsb >= 2, "tc layer: shared-memory plan leaves fewer than 2 weight stages");

@@ -52,6 +52,10 @@ struct TcLayer {
   // only and gather warps copy each tap's A rows into shared memory, instead
   // of the grid form's rows for every input position.
   bool gather = false;
+  // x-run variant of the gathered form: M rows keep whole input x runs (D per
+  // (b, z, y)), so one staged A operand serves the three dx taps by a row
+  // shift; D/Do of the rows are computed for Do outputs.
+  bool xrun = false;
   // device data
   uint8_t* wpk;   // packed weights, blocks [ntile][zt][cg][yx] of nt*128 bytes
   float* bias;    // [cout]

@@ -203,8 +203,9 @@ TcLayer make_tc_layer(int l, bool use_feat) {
     L.nt = 32;
     L.msub = 2;
   }
-  if (l >= 2 && l <= 6) {  // conv3..conv7: M over the valid output positions only
+  if (l >= 2 && l <= 6) {  // conv3..conv7: M over the valid output positions (conv3..conv6: whole x runs)
     L.gather = true;
+    L.xrun = l <= 5;
     L.nt = L.cout == 128 ? 128 : 256;
     L.msub = 2;
   }
@@ -693,9 +694,12 @@ struct Tile {
 };
 constexpr Tile kTiles[] = {{64, 4, TDM_CONV_GRID},   {64, 2, TDM_CONV_GRID},    {128, 2, TDM_CONV_GRID},
                            {128, 1, TDM_CONV_GRID},  {256, 1, TDM_CONV_GRID},   {256, 2, TDM_CONV_GATHER},
-                           {256, 1, TDM_CONV_GATHER}, {128, 2, TDM_CONV_GATHER}};
+                           {256, 1, TDM_CONV_GATHER}, {128, 2, TDM_CONV_GATHER}, {256, 2, TDM_CONV_XRUN},
+                           {256, 1, TDM_CONV_XRUN},   {128, 2, TDM_CONV_XRUN}};
 
-int form_of(const TcLayer& L) { return L.dxf ? TDM_CONV_DXF : L.gather ? TDM_CONV_GATHER : TDM_CONV_GRID; }
+int form_of(const TcLayer& L) {
+  return L.dxf ? TDM_CONV_DXF : L.gather ? (L.xrun ? TDM_CONV_XRUN : TDM_CONV_GATHER) : TDM_CONV_GRID;
+}
 
 // The tcgen05 layer a forward of `net` runs for layer l.
 TcLayer& active_layer(tdm_net* net, int l) {
@@ -719,7 +723,8 @@ std::vector<Tile> tile_candidates(tdm_net* net, int l) {
     TcLayer L = active_layer(net, l);
     L.nt = t.nt;
     L.msub = t.msub;
-    L.gather = t.form == TDM_CONV_GATHER;
+    L.gather = t.form == TDM_CONV_GATHER || t.form == TDM_CONV_XRUN;
+    L.xrun = t.form == TDM_CONV_XRUN;
     if (tc_layer_fits(L)) out.push_back(t);
   }
   return out;
@@ -752,7 +757,10 @@ tdm_status set_tile(tdm_net* net, int l, Tile t) {
   if (L.nt != t.nt || L.msub != t.msub || form_of(L) != t.form) ++net->generation;
   L.nt = t.nt;
   L.msub = t.msub;
-  if (!L.dxf) L.gather = t.form == TDM_CONV_GATHER;
+  if (!L.dxf) {
+    L.gather = t.form == TDM_CONV_GATHER || t.form == TDM_CONV_XRUN;
+    L.xrun = t.form == TDM_CONV_XRUN;
+  }
   return TDM_OK;
 }
 

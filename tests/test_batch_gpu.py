@@ -143,7 +143,7 @@ def test_autotune_keeps_descriptor_bits(tdm, weights, patches, precision):
     for layer, (nt, ms) in tiles.items():
         if layer == "conv2":  # dx-fused: 32 outputs per CTA, N = 96
             assert forms[layer] == "dxf" and nt == 32 and ms in (1, 2), layer
-        elif forms[layer] == "gather":  # one accumulator buffer allowed
+        elif forms[layer] in ("gather", "xrun"):  # one accumulator buffer allowed
             assert layer in ("conv3", "conv4", "conv5", "conv6", "conv7"), layer
             assert (nt, ms) in ((256, 2), (256, 1), (128, 2)), layer
         else:
@@ -155,11 +155,14 @@ def test_autotune_keeps_descriptor_bits(tdm, weights, patches, precision):
 
 
 @pytest.mark.parametrize("layer,tiles", [("conv2", [(32, 2), (32, 1)]),
-                                         ("conv3", [(64, 4), (64, 2), (128, 2), (128, 1), (128, 2, "gather")]),
-                                         ("conv4", [(128, 2, "gather"), (128, 2, "grid")]),
-                                         ("conv5", [(256, 1, "gather"), (128, 2, "gather"), (256, 1, "grid")]),
-                                         ("conv6", [(64, 2), (128, 1), (256, 1), (256, 2, "gather")]),
-                                         ("conv7", [(256, 1, "grid"), (128, 2, "gather"), (256, 1, "gather")]),
+                                         ("conv3", [(64, 4), (64, 2), (128, 2), (128, 1), (128, 2, "gather"),
+                                                    (128, 2, "xrun")]),
+                                         ("conv4", [(128, 2, "gather"), (128, 2, "grid"), (128, 2, "xrun")]),
+                                         ("conv5", [(256, 1, "gather"), (128, 2, "gather"), (256, 1, "grid"),
+                                                    (256, 2, "xrun"), (256, 1, "xrun"), (128, 2, "xrun")]),
+                                         ("conv6", [(64, 2), (128, 1), (256, 1), (256, 2, "gather"), (256, 2, "xrun")]),
+                                         ("conv7", [(256, 1, "grid"), (128, 2, "gather"), (256, 1, "gather"),
+                                                    (256, 2, "xrun"), (128, 2, "xrun")]),
                                          ("conv8", [(64, 4), (128, 2), (256, 1)])])
 def test_every_tile_same_bits(tdm, weights, patches, layer, tiles):
     """Every tile and kernel form of a layer gives the same descriptor bits
@@ -176,7 +179,7 @@ def test_every_tile_same_bits(tdm, weights, patches, layer, tiles):
 
 
 def test_fp8_gather_and_grid_forms_same_bits(tdm, weights, patches):
-    """E4M3 operands: the gathered-row and grid forms of conv3..conv7 agree bit for bit."""
+    """E4M3 operands: the grid, gathered-row and x-run forms of conv3..conv7 agree bit for bit."""
     net = tdm.Net(weights, precision="fp8")
     net.calibrate(patches)
     for layer in ("conv3", "conv4", "conv5", "conv6", "conv7"):
@@ -188,5 +191,8 @@ def test_fp8_gather_and_grid_forms_same_bits(tdm, weights, patches):
     assert np.array_equal(net.forward(patches).cpu().numpy(), ref)
     for layer in ("conv5", "conv6", "conv7"):
         net.set_tile(layer, 256, 2, "gather")
+    assert np.array_equal(net.forward(patches).cpu().numpy(), ref)
+    for layer in ("conv3", "conv4", "conv5", "conv6", "conv7"):
+        net.set_tile(layer, 128, 2, "xrun")
     assert np.array_equal(net.forward(patches).cpu().numpy(), ref)
     tdm.device_status()
