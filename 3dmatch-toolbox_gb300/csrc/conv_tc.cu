@@ -835,6 +835,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
       constexpr uint32_t idesc = ptx::make_idesc(kDxfN, 128, 1, 1);
       const uint32_t lboA = (uint32_t)R * 16u;
       const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), wDesc0 = ptx::smem_desc(sW_u, kDxfN * 16, 128);
+#ifdef TDM_WAIT_STATS
+      long long issue_cycles = 0;  // time inside the MMA issue instruction (a full queue blocks it)
+#endif
       int sa = 0;
       uint32_t pha = 0;
 #ifdef TDM_WAIT_STATS
@@ -865,7 +868,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
 #pragma unroll
               for (int i = 0; i < MSUB; ++i) {
                 const uint64_t adesc = ptx::desc_advance(aRow, (2 * kk) * lboA + (uint32_t)(i * kDxfSub) * 16u);
+#ifdef TDM_WAIT_STATS
+                const long long c_issue = clock64();
+#endif
                 ptx::mma_f16(dbase + i * kDxfN, adesc, bdesc, idesc, accumulate);
+#ifdef TDM_WAIT_STATS
+                issue_cycles += clock64() - c_issue;
+#endif
               }
               accumulate = 1;  // each sub-tile's first MMA (zt = dy = kk = 0) starts its accumulator
             }
@@ -879,6 +888,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
       ptx::mma_commit(done);
       wait_or_flag(done, 0, p.err, DEV_TIMEOUT_MMA);
 #ifdef TDM_WAIT_STATS
+      atomicAdd(&g_wait_stats[2], (unsigned long long)issue_cycles);
       atomicAdd(&g_wait_stats[6], (unsigned long long)(clock64() - t_loop0));
 #endif
     }
