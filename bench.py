@@ -297,6 +297,27 @@ def stage_breakdown(tdm, torch, dev, pair, net, k, ransac_iters, prec, reps=5):
     }
 
 
+def replica_seeds(rank, n_pairs):
+    """Seeds of the synthetic pairs one replica cycles through: every rank
+    registers its own pairs (weak scaling, no data-path collective)."""
+    return [20260000 + 97 * rank + i for i in range(n_pairs)]
+
+
+def max_over_ranks(values, dist, device):
+    """Element-wise maximum of per-rank timings (the slowest replica sets the
+    whole-job time); identity on one process."""
+    import torch
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def job_rate(world, units_per_rank, ms_max):
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return world * units_per_rank / (ms_max / 1000.0)
+
+
 def run_ours(args, rank, world, local):
     import torch
     import __graft_entry__ as ge
@@ -314,7 +335,7 @@ def run_ours(args, rank, world, local):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     k = args.keypoints
-    pairs = [synth.fragment_pair(20260000 + 97 * rank + i, n_points=args.points) for i in range(args.pairs)]
+    pairs = [synth.fragment_pair(sd, n_points=args.points) for sd in replica_seeds(rank, args.pairs)]
     dpairs = [(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)) for a, b, _ in pairs]
     hpairs = [(torch.from_numpy(a).pin_memory().numpy(), torch.from_numpy(b).pin_memory().numpy())
               for a, b, _ in pairs]
@@ -368,10 +389,8 @@ def run_ours(args, rank, world, local):
         barrier()
         ms = e0.elapsed_time(e1)
         wall = (time.perf_counter() - t0) * 1000.0
-        t = torch.tensor([ms, wall], dtype=torch.float64, device=dev)
-        if dist is not None:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t[0]), float(t[1]), res
+        ms, wall = max_over_ranks([ms, wall], dist, dev)
+        return ms, wall, res
 
     prec = args.precision
     net, pipe = make(prec)
@@ -389,11 +408,11 @@ def run_ours(args, rank, world, local):
     net.set_timing(False)
     lt = net.layer_times(reset=True)
     ms_step = ms / args.steps
-    value = world * args.steps / (ms / 1000.0)
+    value = job_rate(world, args.steps, ms)
     # e2e through the host C ABI
     e2e_steps = max(3, args.steps // 2)
     ms_e2e, _, _ = timed(pipe, e2e_steps, host=True)
-    e2e = world * e2e_steps / (ms_e2e / 1000.0)
+    e2e = job_rate(world, e2e_steps, ms_e2e)
     h2d = int(np.mean([(a.shape[0] + b.shape[0]) * 12 for a, b in hpairs]))
     d2h = 12 * 8 + 16 + 4
     # FP32 drop-in form on the same GPU
