@@ -92,7 +92,9 @@ __device__ __forceinline__ bool wait_or_flag(uint32_t bar, uint32_t parity, int*
 // Diagnostic build only: cycles spent in each kind of wait, summed over CTAs.
 // slots: 0 MMA<-accEmpty, 1 MMA<-fullA, 2 MMA<-fullB, 3 producer<-emptyA,
 //        4 producer<-emptyB, 5 epilogue<-accFull, 6 MMA loop total, 7 producer loop total
-__device__ unsigned long long g_wait_stats[8];
+//        (grid and dx-fused kernels); 8..15 the same for the gathered-row kernel,
+//        with 11 = gather warps <- emptyA and 15 = gather loop total
+__device__ unsigned long long g_wait_stats[16];
 #define TDM_TIMED_WAIT(slot, expr)                                           \
   ([&]() {                                                                   \
     long long _c0 = clock64();                                               \
@@ -427,11 +429,17 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-template <int NT, int MSUB, bool FP8, bool XRUN>
+template <int NT, int MSUB, bool FP8, bool XRUN, bool WT>
 __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KParams p) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr int MCTA = MSUB * 128;
-  constexpr uint32_t ACC_COLS = MSUB * NT;
+  // WT (weights as the A operand, 128 output channels): one M = 128 (channels)
+  // x N = MCTA (rows) MMA per K step instead of MSUB M = 128 (rows) x N = 128
+  // ones -- 12 KB of operands per 524k MACs instead of 16 KB.  The accumulator
+  // then holds one channel per TMEM lane and the epilogue transposes through
+  // shared memory.
+  static_assert(!WT || (NT == 128 && !FP8), "weights-as-A form: 128 BF16 output channels");
+  constexpr uint32_t ACC_COLS = WT ? MCTA : MSUB * NT;
   constexpr int NBUF = 2 * ACC_COLS <= 512 ? 2 : 1;  // accumulator buffers
   constexpr uint32_t TMEM_COLS = tmem_cols_for(NBUF * ACC_COLS);
   static_assert(ACC_COLS <= 512, "the accumulator must fit in TMEM");
@@ -445,6 +453,9 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
   uint8_t* sB = smem + NSA * a_stage;
   uint64_t* bars = reinterpret_cast<uint64_t*>(sB + (size_t)nsb * b_stage);
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * NSA + 2 * MAX_NSB + 5);
+  // WT epilogue transposition tiles: per epilogue warp 16 rows x 32 channels of BF16
+  uint16_t* sT = reinterpret_cast<uint16_t*>(
+      (reinterpret_cast<uintptr_t>(tmem_holder + 4) + 15) & ~static_cast<uintptr_t>(15));
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (!__syncthreads_and(aborted(p.err) ? 0 : 1)) return;  // another CTA already failed
@@ -488,7 +499,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
         for (int zt = 0; zt < p.nz && ok; ++zt)
           for (int cg = 0; cg < p.kgroups && ok; ++cg)
             for (int yx = 0; yx < p.nyx; ++yx) {
-              if (!wait_or_flag(emptyB + 8 * sb, phb ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+              if (!TDM_TIMED_WAIT(12, wait_or_flag(emptyB + 8 * sb, phb ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
               ptx::mbar_arrive_expect_tx(fullB + 8 * sb, b_stage);
               armedB[sb] = (int)phb;
               const int64_t blk = (((int64_t)nt * p.nz + zt) * p.kgroups + cg) * p.nyx + yx;
@@ -502,16 +513,21 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
-      constexpr uint32_t idesc = FP8 ? ptx::make_idesc(NT, 128, 0, 0) : ptx::make_idesc(NT, 128, 1, 1);
+      constexpr uint32_t idesc = WT    ? ptx::make_idesc(MCTA, 128, 1, 1)
+                                 : FP8 ? ptx::make_idesc(NT, 128, 0, 0)
+                                       : ptx::make_idesc(NT, 128, 1, 1);
       constexpr uint32_t lboA = RS * 16u;
       const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), bDesc0 = ptx::smem_desc(sB_u, NT * 16, 128);
       int sa = 0, sb = 0;
       uint32_t pha = 0, phb = 0;
       bool ok = true;
+#ifdef TDM_WAIT_STATS
+      const long long t_loop0 = clock64();
+#endif
       uint32_t j = 0;  // tiles done by this CTA
       for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
         const uint32_t buf = j % NBUF, use = j / NBUF;
-        if (!wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA)) break;
+        if (!TDM_TIMED_WAIT(8, wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA))) break;
         ptx::tc_fence_after();
         const uint32_t dbase = tmem + buf * ACC_COLS;
         uint32_t accumulate = 0;
@@ -521,21 +537,25 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
         for (int zt = 0; zt < p.nz && ok; ++zt)
           for (int cg = 0; cg < p.kgroups && ok; ++cg)
             for (int ya = 0; ya < p.nyx / TAPS_PER_A && ok; ++ya) {
-              if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+              if (!TDM_TIMED_WAIT(9, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
               const uint64_t aStage = ptx::desc_advance(aDesc0, sa * a_stage);
               for (int dx = 0; dx < TAPS_PER_A; ++dx) {
-                if (!wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA)) { ok = false; break; }
+                if (!TDM_TIMED_WAIT(10, wait_or_flag(fullB + 8 * sb, phb, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
                 ptx::tc_fence_after();
                 const uint64_t bStage = ptx::desc_advance(bDesc0, sb * b_stage);
                 const uint64_t aTap = ptx::desc_advance(aStage, (uint32_t)dx * 16u);
 #pragma unroll 4
                 for (int kk = 0; kk < cpg / 2; ++kk) {
-                  const uint64_t bdesc = ptx::desc_advance(bStage, (2 * kk) * NT * 16);
+                  const uint64_t wdesc = ptx::desc_advance(bStage, (2 * kk) * NT * 16);
+                  if (WT) {  // D[channel][row] += W[channel][k] . X[row][k]
+                    ptx::mma_f16(dbase, wdesc, ptx::desc_advance(aTap, (2 * kk) * lboA), idesc, accumulate);
+                  } else {
 #pragma unroll
-                  for (int i = 0; i < MSUB; ++i) {
-                    const uint64_t adesc = ptx::desc_advance(aTap, (2 * kk) * lboA + (uint32_t)(i * 128) * 16u);
-                    if (FP8) ptx::mma_f8(dbase + i * NT, adesc, bdesc, idesc, accumulate);
-                    else ptx::mma_f16(dbase + i * NT, adesc, bdesc, idesc, accumulate);
+                    for (int i = 0; i < MSUB; ++i) {
+                      const uint64_t adesc = ptx::desc_advance(aTap, (2 * kk) * lboA + (uint32_t)(i * 128) * 16u);
+                      if (FP8) ptx::mma_f8(dbase + i * NT, adesc, wdesc, idesc, accumulate);
+                      else ptx::mma_f16(dbase + i * NT, adesc, wdesc, idesc, accumulate);
+                    }
                   }
                   accumulate = 1;
                 }
@@ -550,6 +570,9 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
       }
       ptx::mma_commit(done);
       wait_or_flag(done, 0, p.err, DEV_TIMEOUT_MMA);
+#ifdef TDM_WAIT_STATS
+      atomicAdd(&g_wait_stats[14], (unsigned long long)(clock64() - t_loop0));
+#endif
     }
   } else if (warp < 6) {
     // ---------------- epilogue (warps 2-5: TMEM lane quarter warp % 4) ----------------
@@ -560,9 +583,46 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
       const int n0 = (int)(t % p.ntiles) * NT;
       const uint32_t buf = j % NBUF, use = j / NBUF;
       const bool have =
-          __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0) != 0;
+          __all_sync(0xffffffffu, TDM_TIMED_WAIT(13, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE)) ? 1 : 0) != 0;
       if (!have) break;
       ptx::tc_fence_after();
+      if constexpr (WT) {
+        // lane = output channel n0 + 32 q + lane; columns = the tile's rows
+        const float bias_c = __ldg(p.bias + n0 + q * 32 + lane);
+        uint16_t* tw = sT + q * (16 * 32);
+#pragma unroll 1
+        for (int c1 = 0; c1 < MCTA; c1 += 16) {
+          float v[16];
+          ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)c1, v);
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            float a = v[e] + bias_c;
+            if (p.relu) a = fmaxf(a, 0.0f);
+            const __nv_bfloat16 h = __float2bfloat16_rn(a);
+            tw[e * 32 + lane] = *reinterpret_cast<const uint16_t*>(&h);  // [row][channel]
+          }
+          __syncwarp();
+          // 16 rows x 4 chunks of 8 channels: two 16-byte rows per lane
+#pragma unroll
+          for (int k2 = 0; k2 < 2; ++k2) {
+            const int id = lane + 32 * k2, rr = id >> 2, ch = id & 3;
+            const int64_t row = m0 + c1 + rr;
+            bool valid = row < p.rows;
+            int64_t pos;
+            if (XRUN) {
+              const int64_t yz = row / Dx;
+              const int x = (int)(row - yz * Dx);
+              valid = valid && x < p.Do;
+              pos = yz * p.Do + x;  // ((b*Do + z)*Do + y)*Do + x
+            } else {
+              pos = row;
+            }
+            const uint4 val = *reinterpret_cast<const uint4*>(tw + rr * 32 + ch * 8);
+            if (valid) *reinterpret_cast<uint4*>(p.out + (int64_t)(n0 / 8 + q * 4 + ch) * p.out_cs + pos * 16) = val;
+          }
+          __syncwarp();
+        }
+      } else {
 #pragma unroll 1
       for (int i = 0; i < MSUB; ++i) {
         const int64_t row = m0 + i * 128 + q * 32 + lane;
@@ -631,6 +691,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
           }
         }
       }
+      }  // WT / row-major accumulator
       ptx::tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(accEmpty + 8 * buf);
@@ -645,6 +706,9 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
     int q0 = 0, np = 0;
     bool ok = true;
     const int64_t plane = (int64_t)p.D * p.D;
+#ifdef TDM_WAIT_STATS
+    const long long t_loop0 = clock64();
+#endif
     for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
       const int64_t m0 = (t / p.ntiles) * MCTA;
       // this thread's stage rows: gt + 128 i, and in the x-run form also the
@@ -672,7 +736,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
       for (int zt = 0; zt < p.nz && ok; ++zt)
         for (int cg = 0; cg < p.kgroups && ok; ++cg)
           for (int ya = 0; ya < p.nyx / TAPS_PER_A; ++ya) {
-            if (!wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+            if (!TDM_TIMED_WAIT(11, wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
             // tap offset in the input grid (the x-run form stages dx = 0; dx
             // comes from the MMA's row shift)
             const int64_t off = XRUN ? zt * plane + ya * p.D : zt * plane + (ya / 3) * p.D + (ya % 3);
@@ -698,6 +762,9 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
             if (++sa == NSA) { sa = 0; pha ^= 1; }
           }
     }
+#ifdef TDM_WAIT_STATS
+    if (gt == 0) atomicAdd(&g_wait_stats[15], (unsigned long long)(clock64() - t_loop0));
+#endif
     cp_async_wait<0>();  // no copy may still be in flight when the CTA exits
     ptx::fence_proxy_async_smem();
     for (; np > 0; --np) {
@@ -1267,9 +1334,11 @@ size_t gather_stage_bytes(const TcLayer& L) {
   return (size_t)16 * chunks_per_group(L) * (L.msub * 128 + (L.xrun ? 8 : 0));
 }
 int gather_stages(const TcLayer& L) { return L.xrun ? kXNSA : kGNSA; }
+// weights-as-A epilogue: 4 warps x 16 rows x 32 channels of BF16, 16-byte aligned
+constexpr size_t kWtStage = 4 * 16 * 32 * 2 + 16;
 
 int weight_stages(const TcLayer& L) {
-  const size_t a = L.gather ? gather_stages(L) * gather_stage_bytes(L) : NSA * a_stage_bytes(L);
+  const size_t a = L.gather ? gather_stages(L) * gather_stage_bytes(L) + (L.wt ? kWtStage : 0) : NSA * a_stage_bytes(L);
   if (a + kSmemReserve >= kSmemLimit) return 0;
   size_t left = kSmemLimit - kSmemReserve - a;
   int n = (int)(left / ((size_t)L.nt * 128));
@@ -1278,7 +1347,9 @@ int weight_stages(const TcLayer& L) {
 
 size_t smem_bytes(const TcLayer& L) {
   if (L.dxf) return kDxfWBytes + kDxfNSA * a_stage_bytes(L) + kDxfXchg + kDxfStage + 32 + kSmemReserve;
-  if (L.gather) return gather_stages(L) * gather_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
+  if (L.gather)
+    return gather_stages(L) * gather_stage_bytes(L) + (L.wt ? kWtStage : 0) + (size_t)weight_stages(L) * L.nt * 128 +
+           kSmemReserve;
   return NSA * a_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
 }
 
@@ -1312,9 +1383,9 @@ tdm_status launch_t(const KParams& kp, size_t smem, cudaStream_t s) {
   return TDM_OK;
 }
 
-template <int NT, int MSUB, bool FP8, bool XRUN>
+template <int NT, int MSUB, bool FP8, bool XRUN, bool WT = false>
 tdm_status launch_g(const KParams& kp, size_t smem, cudaStream_t s) {
-  auto kern = tc_conv_gather_kernel<NT, MSUB, FP8, XRUN>;
+  auto kern = tc_conv_gather_kernel<NT, MSUB, FP8, XRUN, WT>;
   size_t req = std::max<size_t>(smem, 120 * 1024);
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
@@ -1385,9 +1456,9 @@ tdm_status launch_conv1_tc(const float* patches, int B, const TcLayer& L, uint8_
 #ifdef TDM_WAIT_STATS
 }  // namespace tdm
 extern "C" int tdm_debug_wait_stats(unsigned long long* out, int reset) {
-  if (cudaMemcpyFromSymbol(out, tdm::g_wait_stats, sizeof(unsigned long long) * 8) != cudaSuccess) return 1;
+  if (cudaMemcpyFromSymbol(out, tdm::g_wait_stats, sizeof(unsigned long long) * 16) != cudaSuccess) return 1;
   if (reset) {
-    unsigned long long z[8] = {};
+    unsigned long long z[16] = {};
     if (cudaMemcpyToSymbol(tdm::g_wait_stats, z, sizeof(z)) != cudaSuccess) return 1;
   }
   return 0;
@@ -1405,7 +1476,8 @@ bool tc_layer_fits(const TcLayer& L) {
            L.nyx == 9 && !L.fp8_in && smem_bytes(L) <= kSmemLimit;
   if (L.gather)
     return L.nz == 3 && L.nyx == 9 && L.fp8_in == L.fp8_out && gather_tile_built(L.nt, L.msub) &&
-           L.cout % L.nt == 0 && weight_stages(L) >= 2 && smem_bytes(L) <= kSmemLimit;
+           L.cout % L.nt == 0 && weight_stages(L) >= 2 && smem_bytes(L) <= kSmemLimit &&
+           (!L.wt || (L.nt == 128 && L.msub == 2 && !L.fp8_in && L.cout == 128 && L.out_mode == TC_OUT_C8_CONV));
   return L.nt > 0 && L.msub > 0 && L.cout % L.nt == 0 && 2 * L.msub * L.nt <= 512 && weight_stages(L) >= 2 &&
          smem_bytes(L) <= kSmemLimit;
 }
@@ -1469,6 +1541,7 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
     if (L.xrun) return f8 ? launch_g<NT_, MS_, true, true>(kp, smem, s) : launch_g<NT_, MS_, false, true>(kp, smem, s); \
     return f8 ? launch_g<NT_, MS_, true, false>(kp, smem, s) : launch_g<NT_, MS_, false, false>(kp, smem, s);           \
   }
+    if (L.wt) return L.xrun ? launch_g<128, 2, false, true, true>(kp, smem, s) : launch_g<128, 2, false, false, true>(kp, smem, s);
     TDM_G_CASE(256, 2)
     TDM_G_CASE(256, 1)
     TDM_G_CASE(128, 2)

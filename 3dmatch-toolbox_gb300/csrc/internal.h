@@ -56,6 +56,9 @@ struct TcLayer {
   // (b, z, y)), so one staged A operand serves the three dx taps by a row
   // shift; D/Do of the rows are computed for Do outputs.
   bool xrun = false;
+  // weights as the A operand (128 BF16 output channels, gathered forms): one
+  // 128 x 256 x 16 MMA per K step over both row sub-tiles
+  bool wt = false;
   // device data
   uint8_t* wpk;   // packed weights, blocks [ntile][zt][cg][yx] of nt*128 bytes
   float* bias;    // [cout]

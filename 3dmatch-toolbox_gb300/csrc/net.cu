@@ -206,6 +206,7 @@ TcLayer make_tc_layer(int l, bool use_feat) {
   if (l >= 2 && l <= 6) {  // conv3..conv7: M over the valid output positions (conv3..conv6: whole x runs)
     L.gather = true;
     L.xrun = l <= 5;
+    L.wt = L.cout == 128;  // conv3, conv4: weights as the MMA's A operand (BF16 only)
     L.nt = L.cout == 128 ? 128 : 256;
     L.msub = 2;
   }
@@ -283,6 +284,7 @@ tdm_status setup_weights(tdm_net* net) {
       TcLayer L = make_tc_layer(l, net->use_feat != 0);
       L.fp8_in = true;
       L.fp8_out = l < 7;
+      L.wt = false;  // the weights-as-A form is BF16 only
       const int k_total = l <= 6 ? kCin[l] : 27 * 512;  // K elements per tap (conv) or in total (conv8)
       const int chunks = k_total / 16;
       L.kgroups = chunks < 8 ? 1 : chunks / 8;
@@ -695,10 +697,20 @@ struct Tile {
 constexpr Tile kTiles[] = {{64, 4, TDM_CONV_GRID},   {64, 2, TDM_CONV_GRID},    {128, 2, TDM_CONV_GRID},
                            {128, 1, TDM_CONV_GRID},  {256, 1, TDM_CONV_GRID},   {256, 2, TDM_CONV_GATHER},
                            {256, 1, TDM_CONV_GATHER}, {128, 2, TDM_CONV_GATHER}, {256, 2, TDM_CONV_XRUN},
-                           {256, 1, TDM_CONV_XRUN},   {128, 2, TDM_CONV_XRUN}};
+                           {256, 1, TDM_CONV_XRUN},   {128, 2, TDM_CONV_XRUN},   {128, 2, TDM_CONV_GATHER_WT},
+                           {128, 2, TDM_CONV_XRUN_WT}};
+
+bool form_gathers(int f) {
+  return f == TDM_CONV_GATHER || f == TDM_CONV_XRUN || f == TDM_CONV_GATHER_WT || f == TDM_CONV_XRUN_WT;
+}
+bool form_xrun(int f) { return f == TDM_CONV_XRUN || f == TDM_CONV_XRUN_WT; }
+bool form_wt(int f) { return f == TDM_CONV_GATHER_WT || f == TDM_CONV_XRUN_WT; }
 
 int form_of(const TcLayer& L) {
-  return L.dxf ? TDM_CONV_DXF : L.gather ? (L.xrun ? TDM_CONV_XRUN : TDM_CONV_GATHER) : TDM_CONV_GRID;
+  if (L.dxf) return TDM_CONV_DXF;
+  if (!L.gather) return TDM_CONV_GRID;
+  if (L.wt) return L.xrun ? TDM_CONV_XRUN_WT : TDM_CONV_GATHER_WT;
+  return L.xrun ? TDM_CONV_XRUN : TDM_CONV_GATHER;
 }
 
 // The tcgen05 layer a forward of `net` runs for layer l.
@@ -723,8 +735,9 @@ std::vector<Tile> tile_candidates(tdm_net* net, int l) {
     TcLayer L = active_layer(net, l);
     L.nt = t.nt;
     L.msub = t.msub;
-    L.gather = t.form == TDM_CONV_GATHER || t.form == TDM_CONV_XRUN;
-    L.xrun = t.form == TDM_CONV_XRUN;
+    L.gather = form_gathers(t.form);
+    L.xrun = form_xrun(t.form);
+    L.wt = form_wt(t.form);
     if (tc_layer_fits(L)) out.push_back(t);
   }
   return out;
@@ -758,8 +771,9 @@ tdm_status set_tile(tdm_net* net, int l, Tile t) {
   L.nt = t.nt;
   L.msub = t.msub;
   if (!L.dxf) {
-    L.gather = t.form == TDM_CONV_GATHER || t.form == TDM_CONV_XRUN;
-    L.xrun = t.form == TDM_CONV_XRUN;
+    L.gather = form_gathers(t.form);
+    L.xrun = form_xrun(t.form);
+    L.wt = form_wt(t.form);
   }
   return TDM_OK;
 }

@@ -143,7 +143,7 @@ def test_autotune_keeps_descriptor_bits(tdm, weights, patches, precision):
     for layer, (nt, ms) in tiles.items():
         if layer == "conv2":  # dx-fused: 32 outputs per CTA, N = 96
             assert forms[layer] == "dxf" and nt == 32 and ms in (1, 2), layer
-        elif forms[layer] in ("gather", "xrun"):  # one accumulator buffer allowed
+        elif forms[layer] in ("gather", "xrun", "gather_wt", "xrun_wt"):  # one accumulator buffer allowed
             assert layer in ("conv3", "conv4", "conv5", "conv6", "conv7"), layer
             assert (nt, ms) in ((256, 2), (256, 1), (128, 2)), layer
         else:
@@ -156,8 +156,9 @@ def test_autotune_keeps_descriptor_bits(tdm, weights, patches, precision):
 
 @pytest.mark.parametrize("layer,tiles", [("conv2", [(32, 2), (32, 1)]),
                                          ("conv3", [(64, 4), (64, 2), (128, 2), (128, 1), (128, 2, "gather"),
-                                                    (128, 2, "xrun")]),
-                                         ("conv4", [(128, 2, "gather"), (128, 2, "grid"), (128, 2, "xrun")]),
+                                                    (128, 2, "xrun"), (128, 2, "gather_wt"), (128, 2, "xrun_wt")]),
+                                         ("conv4", [(128, 2, "gather"), (128, 2, "grid"), (128, 2, "xrun"),
+                                                    (128, 2, "xrun_wt"), (128, 2, "gather_wt")]),
                                          ("conv5", [(256, 1, "gather"), (128, 2, "gather"), (256, 1, "grid"),
                                                     (256, 2, "xrun"), (256, 1, "xrun"), (128, 2, "xrun")]),
                                          ("conv6", [(64, 2), (128, 1), (256, 1), (256, 2, "gather"), (256, 2, "xrun")]),
