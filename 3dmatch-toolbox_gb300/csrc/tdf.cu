@@ -46,12 +46,18 @@ __global__ __launch_bounds__(256) void minmax_kernel(const float* __restrict__ p
       mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
     }
   }
-  if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      atomicMin(ws + a, float_to_ordered(mn[a]));
-      atomicMax(ws + 3 + a, float_to_ordered(mx[a]));
-    }
+  // block reduction first: one set of six atomics per block, not per warp
+  __shared__ float s_mn[8][3], s_mx[8][3];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+    for (int a = 0; a < 3; ++a) { s_mn[w][a] = mn[a]; s_mx[w][a] = mx[a]; }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const int a = threadIdx.x;
+    float lo = s_mn[0][a], hi = s_mx[0][a];
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { lo = fminf(lo, s_mn[k][a]); hi = fmaxf(hi, s_mx[k][a]); }
+    atomicMin(ws + a, float_to_ordered(lo));
+    atomicMax(ws + 3 + a, float_to_ordered(hi));
   }
 }
 
@@ -262,7 +268,7 @@ extern "C" tdm_status tdm_grid_from_points(const float* pts, int32_t n, float vs
   int* w = static_cast<int*>(ws);
   minmax_init_kernel<<<1, 32, 0, s>>>(w);
   int blocks = (n + 255) / 256;
-  blocks = blocks > 1216 ? 1216 : blocks;
+  blocks = blocks > 304 ? 304 : blocks;  // two blocks per SM, grid-stride over the points
   minmax_kernel<<<blocks, 256, 0, s>>>(pts, n, w);
   note_launches(1);  // minmax_init_kernel
   TDM_CHECK_LAUNCH("minmax_kernel");

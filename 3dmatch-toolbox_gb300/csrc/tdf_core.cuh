@@ -73,6 +73,8 @@ __device__ __forceinline__ void plane_tile(const uint8_t* __restrict__ occ, int 
   constexpr int ROWS = PB_TY + 2 * R, WPR = (PB_TX + 2 * PB_HALO) / 4, GPR = PB_TX / 4;
   const int64_t X = occ_pitch(dx);
   const int64_t zbase = (int64_t)z * dy * X;
+  const int ngr = (min(PB_TX, dx - x0) + 3) / 4;
+  uint32_t any = 0;
   for (int i = threadIdx.x; i < ROWS * WPR; i += blockDim.x) {
     const int ly = i / WPR, w = i - ly * WPR;
     const int gy = y0 - R + ly, gx = x0 - PB_HALO + 4 * w;
@@ -80,12 +82,28 @@ __device__ __forceinline__ void plane_tile(const uint8_t* __restrict__ occ, int 
     if (gy >= 0 && gy < dy && gx >= 0 && gx < X)
       v = *reinterpret_cast<const uint32_t*>(occ + zbase + (int64_t)gy * X + gx);
     sm.occ[ly][w] = v;
+    any |= v;
   }
-  __syncthreads();
-  const int ngr = (min(PB_TX, dx - x0) + 3) / 4;
+  if (!__syncthreads_or(any != 0)) {
+    // nothing occupied within R of the tile (most tiles of a grid): every
+    // in-plane distance is "none", the value the passes below would produce
+    for (int i = threadIdx.x; i < PB_TY * GPR; i += blockDim.x) {
+      const int ly = i / GPR, g = i - ly * GPR;
+      if (y0 + ly >= dy || g >= ngr) continue;
+      *reinterpret_cast<uint32_t*>(g2 + zbase + (int64_t)(y0 + ly) * X + x0 + 4 * g) = 0xFFFFFFFFu;
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < ROWS * GPR; i += blockDim.x) {
     const int ly = i / GPR, g = i - ly * GPR;
     if (g >= ngr) continue;
+    uint32_t any = 0;  // most of a grid is far from the surface: no occupied byte in the window
+#pragma unroll
+    for (int k = 0; k < 7; ++k) any |= sm.occ[ly][g + k];
+    if (any == 0) {
+      sm.g1[ly][g] = 0xFFFFFFFFu;  // every position: none within R
+      continue;
+    }
     uint32_t mask = 0;  // bit k <-> staged byte 4g + k
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
