@@ -133,9 +133,15 @@ __device__ __forceinline__ void plane_tile(const uint8_t* __restrict__ occ, int 
   for (int i = threadIdx.x; i < PB_TY * GPR; i += blockDim.x) {
     const int ly = i / GPR, g = i - ly * GPR;
     if (y0 + ly >= dy || g >= ngr) continue;
-    uint32_t best = 0xFFFFFFFFu;
+    uint32_t all = 0xFFFFFFFFu;  // every byte "none" in the window: the min-plus gives 0xFF
 #pragma unroll
-    for (int d = -R; d <= R; ++d) best = __vminu4(best, __vaddus4(sm.g1[ly + R + d][g], (uint32_t)(d * d) * 0x01010101u));
+    for (int d = -R; d <= R; ++d) all &= sm.g1[ly + R + d][g];
+    uint32_t best = 0xFFFFFFFFu;
+    if (all != 0xFFFFFFFFu) {
+#pragma unroll
+      for (int d = -R; d <= R; ++d)
+        best = __vminu4(best, __vaddus4(sm.g1[ly + R + d][g], (uint32_t)(d * d) * 0x01010101u));
+    }
     *reinterpret_cast<uint32_t*>(g2 + zbase + (int64_t)(y0 + ly) * X + x0 + 4 * g) = best;
   }
 }
@@ -173,18 +179,33 @@ __device__ __forceinline__ void z_column(const uint8_t* __restrict__ g2, int dx,
   for (int k = 0; k < 2 * R + 1; ++k) ring[k] = word(z0 - R + k);
   const int n = min(128, dx - xseg);
   for (int z = z0; z < z1; ++z) {
+    // the byte-SIMD min-plus is many ALU instructions per word: when every byte
+    // of the window is "none" (0xFF, most of a grid) its result is 0xFF anyway
+    uint32_t all = ring[0];
+#pragma unroll
+    for (int k = 1; k < 2 * R + 1; ++k) all &= ring[k];
     uint32_t best = 0xFFFFFFFFu;
+    if (all != 0xFFFFFFFFu) {
 #pragma unroll
-    for (int k = 0; k < 2 * R + 1; ++k)
-      best = __vminu4(best, __vaddus4(ring[k], (uint32_t)((k - R) * (k - R)) * 0x01010101u));
-#pragma unroll
-    for (int q = 0; q < 4; ++q) s_w[4 * lane + q] = lut[(best >> (8 * q)) & 0xFFu];
-    __syncwarp();
+      for (int k = 0; k < 2 * R + 1; ++k)
+        best = __vminu4(best, __vaddus4(ring[k], (uint32_t)((k - R) * (k - R)) * 0x01010101u));
+    }
     float* out = tdf + ((int64_t)z * dy + y) * dx + xseg;
+    if (__all_sync(0xffffffffu, best == 0xFFFFFFFFu)) {
+      // the whole 128-voxel segment is farther than R from the surface (most
+      // of a grid): TDF 0 (lut[255]), stored without the lookup and staging
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
-      if (lane + 32 * i < n) out[lane + 32 * i] = s_w[lane + 32 * i];
-    __syncwarp();
+      for (int i = 0; i < 4; ++i)
+        if (lane + 32 * i < n) out[lane + 32 * i] = 0.0f;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s_w[4 * lane + q] = lut[(best >> (8 * q)) & 0xFFu];
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (lane + 32 * i < n) out[lane + 32 * i] = s_w[lane + 32 * i];
+      __syncwarp();
+    }
 #pragma unroll
     for (int k = 0; k < 2 * R; ++k) ring[k] = ring[k + 1];
     ring[2 * R] = word(z + R + 1);
