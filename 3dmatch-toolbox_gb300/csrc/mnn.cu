@@ -463,7 +463,9 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
   nn_cols_kernel<<<(nb + 31) / 32, COL_WARPS * 32, 0, s>>>(dot, L.nbp, nb, na, bn, an, maxes, dim, exact, na, cand,
                                                           full, n_full);
   const int64_t lanes = (int64_t)(na + nb) * TOPK;
-  rescore_kernel<<<(unsigned)((lanes + 127) / 128), 128, 0, s>>>(da, db, na, nb, dim, cand, nn_ab, nn_ba);
+  // one warp per block: the FP64 work of 8 queries per warp spreads over every
+  // SM's FP64 pipe instead of packing four warps onto a quarter of the SMs
+  rescore_kernel<<<(unsigned)((lanes + 31) / 32), 32, 0, s>>>(da, db, na, nb, dim, cand, nn_ab, nn_ba);
   note_launches(2);
   if (exact) {
     full_scan_kernel<<<256, 256, 0, s>>>(da, db, na, nb, dim, full, n_full, nn_ab, nn_ba);
