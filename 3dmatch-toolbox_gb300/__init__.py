@@ -364,7 +364,7 @@ class Net:
         valid output positions, A rows gathered per tap) or "xrun" (gathered
         (b, z, y) rows with whole input x runs, the dx taps sharing one operand);
         "gather_wt" / "xrun_wt" put the weights in the MMA's A operand (conv3,
-        conv4 in BF16)."""
+        conv4)."""
         f = np.zeros(9, np.int32)
         check(lib().tdm_net_tile_forms(self.handle, _ptr(f)))
         return {k: self.CONV_FORMS[int(f[i])] for i, k in enumerate(self.LAYER_SLOTS[:9])}

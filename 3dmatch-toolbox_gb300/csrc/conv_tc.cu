@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
   // ones -- 12 KB of operands per 524k MACs instead of 16 KB.  The accumulator
   // then holds one channel per TMEM lane and the epilogue transposes through
   // shared memory.
-  static_assert(!WT || (NT == 128 && !FP8), "weights-as-A form: 128 BF16 output channels");
+  static_assert(!WT || NT == 128, "weights-as-A form: 128 output channels");
   constexpr uint32_t ACC_COLS = WT ? MCTA : MSUB * NT;
   constexpr int NBUF = 2 * ACC_COLS <= 512 ? 2 : 1;  // accumulator buffers
   constexpr uint32_t TMEM_COLS = tmem_cols_for(NBUF * ACC_COLS);
@@ -513,9 +513,8 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
-      constexpr uint32_t idesc = WT    ? ptx::make_idesc(MCTA, 128, 1, 1)
-                                 : FP8 ? ptx::make_idesc(NT, 128, 0, 0)
-                                       : ptx::make_idesc(NT, 128, 1, 1);
+      constexpr uint32_t idesc = WT ? (FP8 ? ptx::make_idesc(MCTA, 128, 0, 0) : ptx::make_idesc(MCTA, 128, 1, 1))
+                                    : (FP8 ? ptx::make_idesc(NT, 128, 0, 0) : ptx::make_idesc(NT, 128, 1, 1));
       constexpr uint32_t lboA = RS * 16u;
       const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), bDesc0 = ptx::smem_desc(sB_u, NT * 16, 128);
       int sa = 0, sb = 0;
@@ -548,7 +547,9 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
                 for (int kk = 0; kk < cpg / 2; ++kk) {
                   const uint64_t wdesc = ptx::desc_advance(bStage, (2 * kk) * NT * 16);
                   if (WT) {  // D[channel][row] += W[channel][k] . X[row][k]
-                    ptx::mma_f16(dbase, wdesc, ptx::desc_advance(aTap, (2 * kk) * lboA), idesc, accumulate);
+                    const uint64_t xdesc = ptx::desc_advance(aTap, (2 * kk) * lboA);
+                    if (FP8) ptx::mma_f8(dbase, wdesc, xdesc, idesc, accumulate);
+                    else ptx::mma_f16(dbase, wdesc, xdesc, idesc, accumulate);
                   } else {
 #pragma unroll
                     for (int i = 0; i < MSUB; ++i) {
@@ -588,24 +589,45 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
       ptx::tc_fence_after();
       if constexpr (WT) {
         // lane = output channel n0 + 32 q + lane; columns = the tile's rows
-        const float bias_c = __ldg(p.bias + n0 + q * 32 + lane);
-        uint16_t* tw = sT + q * (16 * 32);
+        const int c = n0 + q * 32 + lane;
+        const float bias_c = __ldg(p.bias + c);
+        const float scale_c = FP8 ? p.in_scale * __ldg(p.wscale + c) : 1.0f;
+        uint16_t* tw = sT + q * (16 * 32);                 // BF16: [row][channel] halves
+        uint8_t* tb = reinterpret_cast<uint8_t*>(tw);      // E4M3: [row][channel] bytes
 #pragma unroll 1
         for (int c1 = 0; c1 < MCTA; c1 += 16) {
           float v[16];
           ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)c1, v);
 #pragma unroll
           for (int e = 0; e < 16; ++e) {
-            float a = v[e] + bias_c;
+            float a = v[e];
+            if (FP8) a = a * scale_c;
+            a += bias_c;
             if (p.relu) a = fmaxf(a, 0.0f);
-            const __nv_bfloat16 h = __float2bfloat16_rn(a);
-            tw[e * 32 + lane] = *reinterpret_cast<const uint16_t*>(&h);  // [row][channel]
+            v[e] = a;
+          }
+          if (FP8) {
+#pragma unroll
+            for (int e = 0; e < 16; e += 2) {
+              uint16_t pr;
+              asm("cvt.rn.satfinite.e4m3x2.f32 %0, %2, %1;" : "=h"(pr) : "f"(v[e] * p.out_qinv), "f"(v[e + 1] * p.out_qinv));
+              tb[e * 32 + lane] = (uint8_t)(pr & 0xFFu);
+              tb[(e + 1) * 32 + lane] = (uint8_t)(pr >> 8);
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+              const __nv_bfloat16 h = __float2bfloat16_rn(v[e]);
+              tw[e * 32 + lane] = *reinterpret_cast<const uint16_t*>(&h);
+            }
           }
           __syncwarp();
-          // 16 rows x 4 chunks of 8 channels: two 16-byte rows per lane
+          // 16 rows x (BF16: 4 chunks of 8 channels, two per lane; E4M3: 2 chunks of 16, one per lane)
+          constexpr int PER_LANE = FP8 ? 1 : 2;
 #pragma unroll
-          for (int k2 = 0; k2 < 2; ++k2) {
-            const int id = lane + 32 * k2, rr = id >> 2, ch = id & 3;
+          for (int k2 = 0; k2 < PER_LANE; ++k2) {
+            const int id = lane + 32 * k2;
+            const int rr = FP8 ? (id >> 1) : (id >> 2), ch = FP8 ? (id & 1) : (id & 3);
             const int64_t row = m0 + c1 + rr;
             bool valid = row < p.rows;
             int64_t pos;
@@ -617,8 +639,10 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
             } else {
               pos = row;
             }
-            const uint4 val = *reinterpret_cast<const uint4*>(tw + rr * 32 + ch * 8);
-            if (valid) *reinterpret_cast<uint4*>(p.out + (int64_t)(n0 / 8 + q * 4 + ch) * p.out_cs + pos * 16) = val;
+            const uint4 val = FP8 ? *reinterpret_cast<const uint4*>(tb + rr * 32 + ch * 16)
+                                  : *reinterpret_cast<const uint4*>(tw + rr * 32 + ch * 8);
+            const int64_t chunk = FP8 ? (n0 / 16 + q * 2 + ch) : (n0 / 8 + q * 4 + ch);
+            if (valid) *reinterpret_cast<uint4*>(p.out + chunk * p.out_cs + pos * 16) = val;
           }
           __syncwarp();
         }
@@ -1477,7 +1501,7 @@ bool tc_layer_fits(const TcLayer& L) {
   if (L.gather)
     return L.nz == 3 && L.nyx == 9 && L.fp8_in == L.fp8_out && gather_tile_built(L.nt, L.msub) &&
            L.cout % L.nt == 0 && weight_stages(L) >= 2 && smem_bytes(L) <= kSmemLimit &&
-           (!L.wt || (L.nt == 128 && L.msub == 2 && !L.fp8_in && L.cout == 128 && L.out_mode == TC_OUT_C8_CONV));
+           (!L.wt || (L.nt == 128 && L.msub == 2 && L.cout == 128 && L.out_mode == TC_OUT_C8_CONV));
   return L.nt > 0 && L.msub > 0 && L.cout % L.nt == 0 && 2 * L.msub * L.nt <= 512 && weight_stages(L) >= 2 &&
          smem_bytes(L) <= kSmemLimit;
 }
@@ -1541,7 +1565,10 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
     if (L.xrun) return f8 ? launch_g<NT_, MS_, true, true>(kp, smem, s) : launch_g<NT_, MS_, false, true>(kp, smem, s); \
     return f8 ? launch_g<NT_, MS_, true, false>(kp, smem, s) : launch_g<NT_, MS_, false, false>(kp, smem, s);           \
   }
-    if (L.wt) return L.xrun ? launch_g<128, 2, false, true, true>(kp, smem, s) : launch_g<128, 2, false, false, true>(kp, smem, s);
+    if (L.wt) {
+      if (f8) return L.xrun ? launch_g<128, 2, true, true, true>(kp, smem, s) : launch_g<128, 2, true, false, true>(kp, smem, s);
+      return L.xrun ? launch_g<128, 2, false, true, true>(kp, smem, s) : launch_g<128, 2, false, false, true>(kp, smem, s);
+    }
     TDM_G_CASE(256, 2)
     TDM_G_CASE(256, 1)
     TDM_G_CASE(128, 2)

@@ -206,7 +206,7 @@ TcLayer make_tc_layer(int l, bool use_feat) {
   if (l >= 2 && l <= 6) {  // conv3..conv7: M over the valid output positions (conv3..conv6: whole x runs)
     L.gather = true;
     L.xrun = l <= 5;
-    L.wt = L.cout == 128;  // conv3, conv4: weights as the MMA's A operand (BF16 only)
+    L.wt = L.cout == 128;  // conv3, conv4: weights as the MMA's A operand
     L.nt = L.cout == 128 ? 128 : 256;
     L.msub = 2;
   }
@@ -284,7 +284,6 @@ tdm_status setup_weights(tdm_net* net) {
       TcLayer L = make_tc_layer(l, net->use_feat != 0);
       L.fp8_in = true;
       L.fp8_out = l < 7;
-      L.wt = false;  // the weights-as-A form is BF16 only
       const int k_total = l <= 6 ? kCin[l] : 27 * 512;  // K elements per tap (conv) or in total (conv8)
       const int chunks = k_total / 16;
       L.kgroups = chunks < 8 ? 1 : chunks / 8;

@@ -160,8 +160,8 @@ tdm_status tdm_net_set_tile(tdm_net* net, int32_t layer, int32_t nt, int32_t msu
  * (256,2), (256,1), (128,2)); XRUN: gathered (b, z, y) rows with whole input
  * x runs, one staged operand shared by the three dx taps (same layers and
  * tiles); GATHER_WT / XRUN_WT: the same with the weights as the MMA's A
- * operand (M = 128 output channels, N = 256 rows; conv3 and conv4 in BF16,
- * tile (128,2)).  All forms give the same bits. */
+ * operand (M = 128 output channels, N = 256 rows; conv3 and conv4, tile
+ * (128,2)).  All forms give the same bits. */
 typedef enum {
   TDM_CONV_GRID = 0,
   TDM_CONV_DXF = 1,

@@ -196,4 +196,8 @@ def test_fp8_gather_and_grid_forms_same_bits(tdm, weights, patches):
     for layer in ("conv3", "conv4", "conv5", "conv6", "conv7"):
         net.set_tile(layer, 128, 2, "xrun")
     assert np.array_equal(net.forward(patches).cpu().numpy(), ref)
+    for form in ("xrun_wt", "gather_wt"):  # weights as the MMA's A operand, E4M3 output transposed
+        for layer in ("conv3", "conv4"):
+            net.set_tile(layer, 128, 2, form)
+        assert np.array_equal(net.forward(patches).cpu().numpy(), ref), form
     tdm.device_status()
