@@ -43,7 +43,8 @@
 namespace tdm {
 namespace {
 
-constexpr int NSA = 2;      // A slab stages
+constexpr int NSA = 2;      // A slab stages (convolutions)
+constexpr int MAX_NSA = 6;  // A stages of a plain GEMM (conv8, feat, MNN distances): 16 KB each
 constexpr int MAX_NSB = 12;  // B (weight) stages, sized from the shared-memory budget
 constexpr int kThreads = 192;  // warp 0 producer, warp 1 MMA + TMEM owner, warps 2-5 epilogue
 constexpr size_t kSmemLimit = 227 * 1024;
@@ -61,7 +62,7 @@ struct KParams {
   float out_qinv;
   uint8_t* out;
   int64_t out_cs;
-  int D, Do, nz, nyx, kgroups, cpg, cout, out_mode, relu, R, nsb, ntiles;
+  int D, Do, nz, nyx, kgroups, cpg, cout, out_mode, relu, R, nsa, nsb, ntiles;
   int64_t total_tiles;
   int* err;
 };
@@ -164,18 +165,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
   const uint32_t a_stage = 16u * (uint32_t)p.cpg * (uint32_t)R;
   constexpr uint32_t b_stage = NT * 128u;
   uint8_t* sA = smem;
-  uint8_t* sB = smem + NSA * a_stage;
+  const int nsa = p.nsa;  // A stages (more for plain GEMMs, whose stages are small)
+  uint8_t* sB = smem + nsa * a_stage;
   uint64_t* bars = reinterpret_cast<uint64_t*>(sB + (size_t)nsb * b_stage);
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * NSA + 2 * MAX_NSB + 5);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * MAX_NSA + 2 * MAX_NSB + 5);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (!__syncthreads_and(aborted(p.err) ? 0 : 1)) return;  // another CTA already failed
 
-  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * NSA;
-  const uint32_t fullB = emptyA + 8 * NSA, emptyB = fullB + 8 * MAX_NSB;
+  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * MAX_NSA;
+  const uint32_t fullB = emptyA + 8 * MAX_NSA, emptyB = fullB + 8 * MAX_NSB;
   const uint32_t accFull = emptyB + 8 * MAX_NSB, accEmpty = accFull + 16, done = accEmpty + 16;
   if (threadIdx.x == 0) {
-    for (int i = 0; i < NSA; ++i) { ptx::mbar_init(fullA + 8 * i, 1); ptx::mbar_init(emptyA + 8 * i, 1); }
+    for (int i = 0; i < nsa; ++i) { ptx::mbar_init(fullA + 8 * i, 1); ptx::mbar_init(emptyA + 8 * i, 1); }
     for (int i = 0; i < nsb; ++i) { ptx::mbar_init(fullB + 8 * i, 1); ptx::mbar_init(emptyB + 8 * i, 1); }
     for (int i = 0; i < 2; ++i) { ptx::mbar_init(accFull + 8 * i, 1); ptx::mbar_init(accEmpty + 8 * i, 4); }
     ptx::mbar_init(done, 1);
@@ -201,8 +203,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
 #endif
       int sa = 0, sb = 0;
       uint32_t pha = 0, phb = 0;
-      int armedA[NSA], armedB[MAX_NSB];  // parity of each stage's last arming, -1 = never
-      for (int i = 0; i < NSA; ++i) armedA[i] = -1;
+      int armedA[MAX_NSA], armedB[MAX_NSB];  // parity of each stage's last arming, -1 = never
+      for (int i = 0; i < MAX_NSA; ++i) armedA[i] = -1;
       for (int i = 0; i < MAX_NSB; ++i) armedB[i] = -1;
       bool ok = true;
       for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
             const uint8_t* src = p.act + (int64_t)cg * p.cpg * p.act_cs + (m0 + zt * plane) * 16;
             for (int j = 0; j < p.cpg; ++j)
               ptx::bulk_g2s(sA_u + sa * a_stage + j * R * 16, src + j * p.act_cs, R * 16, fullA + 8 * sa);
-            if (++sa == NSA) { sa = 0; pha ^= 1; }
+            if (++sa == nsa) { sa = 0; pha ^= 1; }
             for (int yx = 0; yx < p.nyx; ++yx) {
               if (!TDM_TIMED_WAIT(4, wait_or_flag(emptyB + 8 * sb, phb ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
               ptx::mbar_arrive_expect_tx(fullB + 8 * sb, b_stage);
@@ -233,7 +235,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
       atomicAdd(&g_wait_stats[7], (unsigned long long)(clock64() - t_loop0));
 #endif
       // Drain: every armed stage must have landed before the CTA can exit.
-      for (int i = 0; i < NSA; ++i)
+      for (int i = 0; i < nsa; ++i)
         if (armedA[i] >= 0) wait_or_flag(fullA + 8 * i, (uint32_t)armedA[i], p.err, DEV_TIMEOUT_PRODUCER);
       for (int i = 0; i < nsb; ++i)
         if (armedB[i] >= 0) wait_or_flag(fullB + 8 * i, (uint32_t)armedB[i], p.err, DEV_TIMEOUT_PRODUCER);
@@ -285,7 +287,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
               if (++sb == nsb) { sb = 0; phb ^= 1; }
             }
             ptx::mma_commit(emptyA + 8 * sa);
-            if (++sa == NSA) { sa = 0; pha ^= 1; }
+            if (++sa == nsa) { sa = 0; pha ^= 1; }
           }
         }
         ptx::mma_commit(accFull + 8 * buf);  // fires when this tile's MMAs are complete
@@ -1361,8 +1363,19 @@ int gather_stages(const TcLayer& L) { return L.xrun ? kXNSA : kGNSA; }
 // weights-as-A epilogue: 4 warps x 16 rows x 32 channels of BF16, 16-byte aligned
 constexpr size_t kWtStage = 4 * 16 * 32 * 2 + 16;
 
+// A stages of the grid-form kernel: a GEMM's stage (one K group of msub*128
+// rows) feeds a single weight stage, so as many as fit (up to MAX_NSA, leaving
+// room for four weight stages) stay in flight
+int grid_a_stages(const TcLayer& L) {
+  if (!(L.nz == 1 && L.nyx == 1)) return NSA;
+  const size_t left = kSmemLimit - kSmemReserve - 4 * (size_t)L.nt * 128;
+  const int n = (int)(left / a_stage_bytes(L));
+  return n < NSA ? NSA : (n > MAX_NSA ? MAX_NSA : n);
+}
+
 int weight_stages(const TcLayer& L) {
-  const size_t a = L.gather ? gather_stages(L) * gather_stage_bytes(L) + (L.wt ? kWtStage : 0) : NSA * a_stage_bytes(L);
+  const size_t a = L.gather ? gather_stages(L) * gather_stage_bytes(L) + (L.wt ? kWtStage : 0)
+                            : grid_a_stages(L) * a_stage_bytes(L);
   if (a + kSmemReserve >= kSmemLimit) return 0;
   size_t left = kSmemLimit - kSmemReserve - a;
   int n = (int)(left / ((size_t)L.nt * 128));
@@ -1374,7 +1387,7 @@ size_t smem_bytes(const TcLayer& L) {
   if (L.gather)
     return gather_stages(L) * gather_stage_bytes(L) + (L.wt ? kWtStage : 0) + (size_t)weight_stages(L) * L.nt * 128 +
            kSmemReserve;
-  return NSA * a_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
+  return grid_a_stages(L) * a_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
 }
 
 int sm_count() {
@@ -1576,6 +1589,7 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
     return fail(TDM_ERR_UNSUPPORTED, "tc layer: unsupported gathered-row tile");
   }
   kp.nsb = weight_stages(L);
+  kp.nsa = grid_a_stages(L);
   TDM_REQUIRE(kp.nsb >= 2, "tc layer: shared-memory plan leaves fewer than 2 weight stages");
   TDM_REQUIRE(smem_bytes(L) <= kSmemLimit, "tc layer: shared-memory plan exceeds 227 KB");
   TDM_REQUIRE(L.cout % L.nt == 0, "tc layer: cout must be a multiple of the N tile");
