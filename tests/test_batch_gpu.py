@@ -201,3 +201,25 @@ def test_fp8_gather_and_grid_forms_same_bits(tdm, weights, patches):
             net.set_tile(layer, 128, 2, form)
         assert np.array_equal(net.forward(patches).cpu().numpy(), ref), form
     tdm.device_status()
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp8"])
+def test_gathered_forms_small_batches(tdm, weights, patches, precision):
+    """Tiny and ragged batches (one tile, partial tiles, x-run padding rows past
+    the end) give every patch the bits it gets in a full batch, in every form."""
+    net = tdm.Net(weights, precision=precision)
+    if precision == "fp8":
+        net.calibrate(patches)
+    full = net.forward(patches).cpu().numpy()
+    forms = [("gather", (128, 2), (256, 2)), ("xrun", (128, 2), (256, 2)), ("xrun_wt", (128, 2), None),
+             ("gather_wt", (128, 2), None)]
+    for form, t128, t256 in forms:
+        for layer in ("conv3", "conv4", "conv5", "conv6", "conv7"):
+            t = t128 if layer in ("conv3", "conv4") else t256
+            if t is None:
+                continue
+            net.set_tile(layer, t[0], t[1], form)
+        for lo, hi in ((7, 8), (0, 3), (100, 137)):
+            got = net.forward(patches[lo:hi].contiguous()).cpu().numpy()
+            assert np.array_equal(got, full[lo:hi]), (form, lo, hi)
+    tdm.device_status()
