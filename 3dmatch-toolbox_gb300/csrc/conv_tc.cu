@@ -417,7 +417,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
 // the same sum taken in the same order.
 // ---------------------------------------------------------------------------
 constexpr int kGWarps = 4;                          // gather warps (warps 6..9)
-constexpr int kGThreads = kThreads + 32 * kGWarps;
+// warps 10..13: a second set of epilogue warps (each lane quarter drains its
+// accumulator in two column halves), so a single-buffered tile frees TMEM sooner
+constexpr int kGThreads = kThreads + 32 * kGWarps + 128;
 constexpr int kGNSA = 4;                            // A stages (gathered rows)
 constexpr int kXNSA = 3;                            // A stages (x runs: three B stages per A stage)
 
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
   uint8_t* sB = smem + NSA * a_stage;
   uint64_t* bars = reinterpret_cast<uint64_t*>(sB + (size_t)nsb * b_stage);
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * NSA + 2 * MAX_NSB + 5);
-  // WT epilogue transposition tiles: per epilogue warp 16 rows x 32 channels of BF16
+  // WT epilogue transposition tiles: per epilogue warp (8) 16 rows x 32 channels of BF16
   uint16_t* sT = reinterpret_cast<uint16_t*>(
       (reinterpret_cast<uintptr_t>(tmem_holder + 4) + 15) & ~static_cast<uintptr_t>(15));
 
@@ -471,7 +473,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
       ptx::mbar_init(emptyA + 8 * i, 1);
     }
     for (int i = 0; i < nsb; ++i) { ptx::mbar_init(fullB + 8 * i, 1); ptx::mbar_init(emptyB + 8 * i, 1); }
-    for (int i = 0; i < 2; ++i) { ptx::mbar_init(accFull + 8 * i, 1); ptx::mbar_init(accEmpty + 8 * i, 4); }
+    for (int i = 0; i < 2; ++i) { ptx::mbar_init(accFull + 8 * i, 1); ptx::mbar_init(accEmpty + 8 * i, 8); }
     ptx::mbar_init(done, 1);
     ptx::fence_barrier_init();
     ptx::fence_proxy_async_smem();
@@ -577,9 +579,10 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
       atomicAdd(&g_wait_stats[14], (unsigned long long)(clock64() - t_loop0));
 #endif
     }
-  } else if (warp < 6) {
-    // ---------------- epilogue (warps 2-5: TMEM lane quarter warp % 4) ----------------
-    const int q = warp & 3;
+  } else if (warp < 6 || warp >= 10) {
+    // ---------------- epilogue (warps 2-5 and 10-13: TMEM lane quarter warp % 4,
+    // column half eh) ----------------
+    const int q = warp & 3, eh = warp >= 10 ? 1 : 0;
     uint32_t j = 0;
     for (int64_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
       const int64_t m0 = (t / p.ntiles) * MCTA;
@@ -594,10 +597,10 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
         const int c = n0 + q * 32 + lane;
         const float bias_c = __ldg(p.bias + c);
         const float scale_c = FP8 ? p.in_scale * __ldg(p.wscale + c) : 1.0f;
-        uint16_t* tw = sT + q * (16 * 32);                 // BF16: [row][channel] halves
+        uint16_t* tw = sT + (eh * 4 + q) * (16 * 32);      // BF16: [row][channel] halves
         uint8_t* tb = reinterpret_cast<uint8_t*>(tw);      // E4M3: [row][channel] bytes
 #pragma unroll 1
-        for (int c1 = 0; c1 < MCTA; c1 += 16) {
+        for (int c1 = eh * (MCTA / 2); c1 < (eh + 1) * (MCTA / 2); c1 += 16) {
           float v[16];
           ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)c1, v);
 #pragma unroll
@@ -667,7 +670,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
         }
         pos = b * Do3 + tap;
 #pragma unroll 1
-        for (int c1 = 0; c1 < NT; c1 += 32) {
+        for (int c1 = eh * (NT / 2); c1 < (eh + 1) * (NT / 2); c1 += 32) {
           uint32_t r2[2][16];  // 32 accumulator columns: two loads, one wait
           const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)(i * NT + c1);
           ptx::tmem_ld16_nowait(ta, r2[0]);
@@ -1360,8 +1363,8 @@ size_t gather_stage_bytes(const TcLayer& L) {
   return (size_t)16 * chunks_per_group(L) * (L.msub * 128 + (L.xrun ? 8 : 0));
 }
 int gather_stages(const TcLayer& L) { return L.xrun ? kXNSA : kGNSA; }
-// weights-as-A epilogue: 4 warps x 16 rows x 32 channels of BF16, 16-byte aligned
-constexpr size_t kWtStage = 4 * 16 * 32 * 2 + 16;
+// weights-as-A epilogue: 8 warps x 16 rows x 32 channels of BF16, 16-byte aligned
+constexpr size_t kWtStage = 8 * 16 * 32 * 2 + 16;
 
 // A stages of the grid-form kernel: a GEMM's stage (one K group of msub*128
 // rows) feeds a single weight stage, so as many as fit (up to MAX_NSA, leaving
