@@ -839,7 +839,12 @@ constexpr int kDxfNSA = 2;  // A slab stages
 
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 
-template <int MSUB, bool FP8_OUT>
+// XPOOL: the epilogue also takes the max of each x pair (the first step of
+// the 2x2x2 max-pool that follows conv2) and writes x extent Do/2.  Adjacent x
+// are adjacent TMEM lanes, every sub-tile starts and ends on an even x (D, Do,
+// 126 and the tile starts are even), and max commutes with the monotonic BF16
+// and E4M3 rounding, so the pool's result is the same bits.
+template <int MSUB, bool FP8_OUT, bool XPOOL>
 __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams p) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr int MOUT = MSUB * kDxfSub;
@@ -1077,6 +1082,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
             const float a = ((__uint_as_float(r0[e]) + s1) + s2) + bi[e];
             v[e] = p.relu ? fmaxf(a, 0.0f) : a;
           }
+          // staging row: the lane's row, or in the x-pooled form the pair's (even
+          // lanes store the max of the packed values of lanes L and L ^ 1; the
+          // rounding is monotonic, so packing first gives the same bits)
+          const bool stage = !XPOOL || (L & 1) == 0;
+          const int SL = XPOOL ? (L >> 1) : L;
           // rows 126 and 127 of a sub-tile are staged too but never stored
           if (FP8_OUT) {
             uint4 o;
@@ -1084,7 +1094,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
             o.y = pack_e4m3x4(v[4] * p.out_qinv, v[5] * p.out_qinv, v[6] * p.out_qinv, v[7] * p.out_qinv);
             o.z = pack_e4m3x4(v[8] * p.out_qinv, v[9] * p.out_qinv, v[10] * p.out_qinv, v[11] * p.out_qinv);
             o.w = pack_e4m3x4(v[12] * p.out_qinv, v[13] * p.out_qinv, v[14] * p.out_qinv, v[15] * p.out_qinv);
-            *reinterpret_cast<uint4*>(sO + ((i * 4 + c0 / 16) * 128 + L) * 16) = o;
+            if (XPOOL) {  // ReLU outputs: E4M3 bytes order like the values
+              o.x = __vmaxu4(o.x, __shfl_xor_sync(0xffffffffu, o.x, 1));
+              o.y = __vmaxu4(o.y, __shfl_xor_sync(0xffffffffu, o.y, 1));
+              o.z = __vmaxu4(o.z, __shfl_xor_sync(0xffffffffu, o.z, 1));
+              o.w = __vmaxu4(o.w, __shfl_xor_sync(0xffffffffu, o.w, 1));
+            }
+            if (stage) *reinterpret_cast<uint4*>(sO + ((i * 4 + c0 / 16) * 128 + SL) * 16) = o;
           } else {
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -1093,7 +1109,17 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
               o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
               o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
               o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
-              *reinterpret_cast<uint4*>(sO + ((i * 4 + c0 / 8 + h) * 128 + L) * 16) = o;
+              if (XPOOL) {
+                uint32_t* w = reinterpret_cast<uint32_t*>(&o);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                  const uint32_t nb = __shfl_xor_sync(0xffffffffu, w[k], 1);
+                  __nv_bfloat162 m = __hmax2(*reinterpret_cast<const __nv_bfloat162*>(&w[k]),
+                                             *reinterpret_cast<const __nv_bfloat162*>(&nb));
+                  w[k] = *reinterpret_cast<uint32_t*>(&m);
+                }
+              }
+              if (stage) *reinterpret_cast<uint4*>(sO + ((i * 4 + c0 / 8 + h) * 128 + SL) * 16) = o;
             }
           }
         }
@@ -1118,12 +1144,15 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
           const int z = (int)(bz - b * p.D);
           if (y < p.Do && z < p.Do) {
             const int x = (int)(ra - yr * p.D);
-            const int64_t pout = ((b * p.Do + z) * p.Do + y) * p.Do + x;
-            const uint32_t len = (uint32_t)(rb - ra) * 16u;
+            // x-pooled: x pairs (ra and rb are even), row pitch Do/2
+            const int XO = XPOOL ? p.Do / 2 : p.Do;
+            const int64_t pout = ((b * p.Do + z) * p.Do + y) * XO + (XPOOL ? x / 2 : x);
+            const uint32_t len = (uint32_t)((rb - ra) / (XPOOL ? 2 : 1)) * 16u;
+            const int srow = (int)(ra - s0) / (XPOOL ? 2 : 1);
 #pragma unroll
             for (int c = 0; c < CH; ++c)
               ptx::bulk_s2g(p.out + (int64_t)(n0 / (FP8_OUT ? 16 : 8) + c) * p.out_cs + pout * 16,
-                            sO_u + ((q * 4 + c) * 128 + (int)(ra - s0)) * 16, len);
+                            sO_u + ((q * 4 + c) * 128 + srow) * 16, len);
             ptx::bulk_commit();
             issued = true;
           }
@@ -1444,9 +1473,9 @@ bool gather_tile_built(int nt, int msub) {
   return (nt == 256 && (msub == 1 || msub == 2)) || (nt == 128 && msub == 2);
 }
 
-template <int MSUB, bool FP8_OUT>
+template <int MSUB, bool FP8_OUT, bool XPOOL>
 tdm_status launch_dxf(const KParams& kp, size_t smem, cudaStream_t s) {
-  auto kern = tc_conv_dxf_kernel<MSUB, FP8_OUT>;
+  auto kern = tc_conv_dxf_kernel<MSUB, FP8_OUT, XPOOL>;
   size_t req = std::max<size_t>(smem, 120 * 1024);
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
@@ -1557,8 +1586,16 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
     kp.nsb = 0;
     kp.total_tiles = ((a.rows + mout - 1) / mout) * 2;
     const size_t smem = smem_bytes(L);
-    if (L.msub == 2) return L.fp8_out ? launch_dxf<2, true>(kp, smem, s) : launch_dxf<2, false>(kp, smem, s);
-    return L.fp8_out ? launch_dxf<1, true>(kp, smem, s) : launch_dxf<1, false>(kp, smem, s);
+    TDM_REQUIRE(!a.xpool || (L.D % 2 == 0 && L.Do % 2 == 0), "tc layer: x-pooled output needs even extents");
+#define TDM_DXF(MS_, F8_)                                                                       \
+    return a.xpool ? launch_dxf<MS_, F8_, true>(kp, smem, s) : launch_dxf<MS_, F8_, false>(kp, smem, s)
+    if (L.msub == 2) {
+      if (L.fp8_out) TDM_DXF(2, true);
+      TDM_DXF(2, false);
+    }
+    if (L.fp8_out) TDM_DXF(1, true);
+    TDM_DXF(1, false);
+#undef TDM_DXF
   }
   if (L.gather) {
     TDM_REQUIRE(tc_layer_fits(L), "tc layer: unsupported gathered-row tile");

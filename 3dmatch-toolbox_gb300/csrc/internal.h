@@ -17,10 +17,11 @@ tdm_status launch_conv1(const float* patches, int B, const float* w, const float
 tdm_status launch_conv_f32(const float* in, int B, int D, int C, int ks, const float* w, const float* bias, int K,
                            bool relu, float* out, cudaStream_t s);
 tdm_status launch_pool_f32(const float* in, int B, int D, int C, float* out, cudaStream_t s);
+// x_pooled: the input's x extent is already D/2 (max of x pairs, from conv2's epilogue)
 tdm_status launch_pool_c16_u8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out,
-                              int64_t out_cs, cudaStream_t s);
+                              int64_t out_cs, cudaStream_t s, bool x_pooled = false);
 tdm_status launch_pool_c8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out, int64_t out_cs,
-                          cudaStream_t s);
+                          cudaStream_t s, bool x_pooled = false);
 
 // ---- conv_tc.cu: tcgen05 implicit-GEMM convolution / GEMM ----
 // Output layouts of the tensor-core epilogue.
@@ -73,6 +74,7 @@ struct TcArgs {
   int64_t out_cs;  // bytes between output chunks
   float in_scale;  // FP8: activation dequantisation scale of the input
   float out_qinv;  // FP8 output: 1/scale used to quantise
+  bool xpool = false;  // dx-fused conv2: write the max of each x pair (x extent Do/2)
 };
 
 // Rows of slack a chunk-planar input needs after its last row for layer L.

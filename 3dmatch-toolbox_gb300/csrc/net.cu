@@ -451,6 +451,8 @@ tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, in
       out_cs = ((int64_t)B * 17576 + 8) * 16;  // conv2 output, read by the pool
       a.out = dst;
       a.out_cs = out_cs;
+      // the epilogue takes the pool's x-pair max unless conv2's own response is wanted
+      a.xpool = stop != 1 && L.dxf;
     } else {
       out_cs = P.rows_alloc[l + 1] * 16;
       a.out = dst;
@@ -469,8 +471,8 @@ tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, in
     if (l == 1) {  // pool 26^3 -> 13^3 back into buffer 0 as conv3's input
       int64_t pcs = P.rows_alloc[2] * 16;
       ev = net->begin(9, s);
-      st = fp8 ? launch_pool_c16_u8(dst, out_cs, B, 26, 4, cur, pcs, s)
-               : launch_pool_c8(dst, out_cs, B, 26, 8, cur, pcs, s);
+      st = fp8 ? launch_pool_c16_u8(dst, out_cs, B, 26, 4, cur, pcs, s, a.xpool)
+               : launch_pool_c8(dst, out_cs, B, 26, 8, cur, pcs, s, a.xpool);
       net->end(ev, s);
       if (st) return st;
       if (stop == kPool) {
