@@ -63,6 +63,8 @@ struct KParams {
   uint8_t* out;
   int64_t out_cs;
   int D, Do, nz, nyx, kgroups, cpg, cout, out_mode, relu, R, nsa, nsb, ntiles;
+  int ksplit;   // K splits of a GEMM (tiles ordered m, n, split); > 1: raw FP32 partials to part
+  float* part;  // [ksplit][rows][cout] when ksplit > 1
   int64_t total_tiles;
   int* err;
 };
@@ -208,11 +210,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
       for (int i = 0; i < MAX_NSB; ++i) armedB[i] = -1;
       bool ok = true;
       for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
-        const int64_t m0 = (t / p.ntiles) * MCTA;
-        const int nt = (int)(t % p.ntiles);
+        const int64_t m0 = (t / ((int64_t)p.ntiles * p.ksplit)) * MCTA;
+        const int nt = (int)((t / p.ksplit) % p.ntiles);
+        const int kg = p.kgroups / p.ksplit, cg0 = (int)(t % p.ksplit) * kg;
         if (!tile_has_work(p, m0, MCTA)) continue;
         for (int zt = 0; zt < p.nz && ok; ++zt) {
-          for (int cg = 0; cg < p.kgroups && ok; ++cg) {
+          for (int cg = cg0; cg < cg0 + kg && ok; ++cg) {
             if (!TDM_TIMED_WAIT(3, wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
             ptx::mbar_arrive_expect_tx(fullA + 8 * sa, a_stage);
             armedA[sa] = (int)pha;
@@ -254,7 +257,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
       const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), bDesc0 = ptx::smem_desc(sB_u, NT * 16, 128);
       uint32_t j = 0;  // tiles done by this CTA
       for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
-        const int64_t m0 = (t / p.ntiles) * MCTA;
+        const int64_t m0 = (t / ((int64_t)p.ntiles * p.ksplit)) * MCTA;
+        const int kg = p.kgroups / p.ksplit;
         if (!tile_has_work(p, m0, MCTA)) continue;
         const uint32_t buf = j & 1u, use = j >> 1;
         if (!TDM_TIMED_WAIT(0, wait_or_flag(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
@@ -262,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
         const uint32_t dbase = tmem + buf * ACC_COLS;
         uint32_t accumulate = 0;
         for (int zt = 0; zt < p.nz && ok; ++zt) {
-          for (int cg = 0; cg < p.kgroups && ok; ++cg) {
+          for (int cg = 0; cg < kg && ok; ++cg) {
             if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
             ptx::tc_fence_after();
             const uint64_t aStage = ptx::desc_advance(aDesc0, sa * a_stage);
@@ -305,8 +309,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
     const int64_t D3 = (int64_t)p.D * p.D * p.D;
     uint32_t j = 0;
     for (int64_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
-      const int64_t m0 = (t / p.ntiles) * MCTA;
-      const int n0 = (int)(t % p.ntiles) * NT;
+      const int64_t m0 = (t / ((int64_t)p.ntiles * p.ksplit)) * MCTA;
+      const int n0 = (int)((t / p.ksplit) % p.ntiles) * NT;
+      const int ks = (int)(t % p.ksplit);
       if (!tile_has_work(p, m0, MCTA)) continue;
       const uint32_t buf = j & 1u, use = j >> 1;
       const bool have =
@@ -335,6 +340,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
           ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + (uint32_t)(i * NT + c0), v);
           if (!valid) continue;
           const int n = n0 + c0;
+          if (p.ksplit > 1) {  // raw partial sums; splitk_reduce_kernel finishes the layer
+            float4* dst = reinterpret_cast<float4*>(p.part + ((int64_t)ks * p.rows + row) * p.cout + n);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) dst[h] = make_float4(v[4 * h], v[4 * h + 1], v[4 * h + 2], v[4 * h + 3]);
+            continue;
+          }
           float bs[16], sc[16];
           load16(p.bias + n, bs);
           if (FP8_IN) load16(p.wscale + n, sc);
@@ -399,6 +410,49 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const KParams p) {
   if (warp == 1) {
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+// Split-K GEMM finish: out = act(sum_s part[s] (s in order) * scale + bias) for
+// 8 channels of one row per thread, in the layer's output format.
+template <bool FP8_IN>
+__global__ __launch_bounds__(256) void splitk_reduce_kernel(const float* __restrict__ part, int ksplit, int64_t rows,
+                                                            int cout, const float* __restrict__ bias,
+                                                            const float* __restrict__ wscale, float in_scale, int relu,
+                                                            int out_mode, uint8_t* __restrict__ out, int64_t out_cs) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int groups = cout / 8;
+  if (i >= rows * groups) return;
+  const int64_t row = i / groups;
+  const int n = (int)(i - row * groups) * 8;
+  float v[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) v[e] = 0.0f;
+  for (int k = 0; k < ksplit; ++k) {
+    const float4* src = reinterpret_cast<const float4*>(part + ((int64_t)k * rows + row) * cout + n);
+    const float4 a = __ldg(src), b = __ldg(src + 1);
+    v[0] += a.x; v[1] += a.y; v[2] += a.z; v[3] += a.w;
+    v[4] += b.x; v[5] += b.y; v[6] += b.z; v[7] += b.w;
+  }
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    float a = v[e];
+    if (FP8_IN) a = a * (in_scale * __ldg(wscale + n + e));
+    a += __ldg(bias + n + e);
+    if (relu) a = fmaxf(a, 0.0f);
+    v[e] = a;
+  }
+  if (out_mode == TC_OUT_F32_ROWS) {
+    float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(out) + row * cout + n);
+    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+  } else {  // TC_OUT_C8_ROWS: BF16 chunk n / 8, row = input row
+    uint4 o;
+    o.x = pack_bf16x2(v[0], v[1]);
+    o.y = pack_bf16x2(v[2], v[3]);
+    o.z = pack_bf16x2(v[4], v[5]);
+    o.w = pack_bf16x2(v[6], v[7]);
+    *reinterpret_cast<uint4*>(out + (int64_t)(n / 8) * out_cs + row * 16) = o;
   }
 }
 
@@ -1630,6 +1684,11 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   }
   kp.nsb = weight_stages(L);
   kp.nsa = grid_a_stages(L);
+  kp.ksplit = L.ksplit > 1 ? L.ksplit : 1;
+  kp.part = a.part;
+  TDM_REQUIRE(kp.ksplit == 1 || (L.nz == 1 && L.nyx == 1 && L.kgroups % kp.ksplit == 0 && a.part &&
+                                 (L.out_mode == TC_OUT_F32_ROWS || (L.out_mode == TC_OUT_C8_ROWS && !L.fp8_out))),
+              "tc layer: split-K needs a plain GEMM, K groups divisible by the splits, a partial buffer, F32 or BF16 rows");
   TDM_REQUIRE(kp.nsb >= 2, "tc layer: shared-memory plan leaves fewer than 2 weight stages");
   TDM_REQUIRE(smem_bytes(L) <= kSmemLimit, "tc layer: shared-memory plan exceeds 227 KB");
   TDM_REQUIRE(L.cout % L.nt == 0, "tc layer: cout must be a multiple of the N tile");
@@ -1640,9 +1699,29 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   const int64_t mcta = (int64_t)L.msub * 128;
   const int64_t mtiles = (a.rows + mcta - 1) / mcta;
   kp.ntiles = L.cout / L.nt;
-  kp.total_tiles = mtiles * kp.ntiles;
+  kp.total_tiles = mtiles * kp.ntiles * kp.ksplit;
   const size_t smem = smem_bytes(L);
   const bool f8i = L.fp8_in, f8o = L.fp8_out;
+  if (kp.ksplit > 1) {
+    tdm_status st = TDM_OK;
+#define TDM_TC_SPLIT(NT_, MS_)                                                                         \
+    if (L.nt == NT_ && L.msub == MS_) st = f8i ? launch_t<NT_, MS_, true, false>(kp, smem, s)          \
+                                               : launch_t<NT_, MS_, false, false>(kp, smem, s);       \
+    else
+    TDM_TC_SPLIT(64, 4) TDM_TC_SPLIT(64, 2) TDM_TC_SPLIT(128, 2) TDM_TC_SPLIT(128, 1) TDM_TC_SPLIT(256, 1)
+    return fail(TDM_ERR_UNSUPPORTED, "tc layer: unsupported (nt, msub) tile");
+#undef TDM_TC_SPLIT
+    if (st) return st;
+    const int64_t n = a.rows * (L.cout / 8);
+    if (f8i)
+      splitk_reduce_kernel<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+          a.part, kp.ksplit, a.rows, L.cout, L.bias, L.wscale, a.in_scale, L.relu, L.out_mode, a.out, a.out_cs);
+    else
+      splitk_reduce_kernel<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+          a.part, kp.ksplit, a.rows, L.cout, L.bias, L.wscale, a.in_scale, L.relu, L.out_mode, a.out, a.out_cs);
+    TDM_CHECK_LAUNCH("splitk_reduce_kernel");
+    return TDM_OK;
+  }
 #define TDM_TC_CASE(NT_, MS_)                                                                  \
   if (L.nt == NT_ && L.msub == MS_) {                                                          \
     if (f8i && f8o) return launch_t<NT_, MS_, true, true>(kp, smem, s);                        \

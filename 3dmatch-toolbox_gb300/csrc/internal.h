@@ -60,6 +60,10 @@ struct TcLayer {
   // weights as the A operand (128 BF16 output channels, gathered forms): one
   // 128 x 256 x 16 MMA per K step over both row sub-tiles
   bool wt = false;
+  // K splits of a plain GEMM (conv8): each tile accumulates one K range into
+  // FP32 partials and a reduce pass adds them in order (more CTAs for a
+  // 2,048-row GEMM with K = 13,824)
+  int ksplit = 1;
   // device data
   uint8_t* wpk;   // packed weights, blocks [ntile][zt][cg][yx] of nt*128 bytes
   float* bias;    // [cout]
@@ -75,6 +79,7 @@ struct TcArgs {
   float in_scale;  // FP8: activation dequantisation scale of the input
   float out_qinv;  // FP8 output: 1/scale used to quantise
   bool xpool = false;  // dx-fused conv2: write the max of each x pair (x extent Do/2)
+  float* part = nullptr;  // split-K partial sums, [ksplit][rows][cout] FP32
 };
 
 // Rows of slack a chunk-planar input needs after its last row for layer L.

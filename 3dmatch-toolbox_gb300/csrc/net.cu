@@ -172,6 +172,8 @@ namespace {
 
 int64_t round16(int64_t x) { return (x + 15) & ~(int64_t)15; }
 
+constexpr int kConv8Splits = 4;  // conv8's K splits (divides its 216 BF16 / 108 E4M3 K groups)
+
 TcLayer make_tc_layer(int l, bool use_feat) {
   TcLayer L{};
   L.cin = kCin[l];
@@ -192,6 +194,7 @@ TcLayer make_tc_layer(int l, bool use_feat) {
     L.nyx = 1;
     L.kgroups = (l == 7 ? 27 * 512 : 512) / 64;
     L.out_mode = (l == 7 && use_feat) ? TC_OUT_C8_ROWS : TC_OUT_F32_ROWS;
+    L.ksplit = l == 7 ? kConv8Splits : 1;  // conv8: K = 13,824 over only cout/nt x rows/128 tiles
   }
   // N tile and M sub-tiles per CTA; two accumulator buffers of msub*nt TMEM
   // columns each must fit in 512 columns.
@@ -369,6 +372,7 @@ struct Bf16Plan {
   int64_t rows_alloc[9];  // rows allocated per chunk for the input of layer l
   int64_t rows[9];        // live rows of the input of layer l
   size_t off1;            // byte offset of buffer 1
+  size_t off_part;        // conv8's split-K partial sums
   size_t total;
 };
 
@@ -390,7 +394,8 @@ Bf16Plan bf16_plan(const tdm_net* net, int B) {
   for (int l : {3, 5}) b1 = std::max(b1, (size_t)chunks(l) * P.rows_alloc[l] * 16);
   b1 = std::max(b1, (size_t)1728 * P.rows_alloc[7] * 16);  // conv7 -> conv8 flattened operand
   P.off1 = round16((int64_t)b0) + 4096;
-  P.total = P.off1 + b1 + 4096;
+  P.off_part = P.off1 + round16((int64_t)b1) + 4096;
+  P.total = P.off_part + (size_t)kConv8Splits * B * 512 * sizeof(float) + 4096;
   return P;
 }
 
@@ -443,6 +448,7 @@ tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, in
     a.rows = P.rows[l];
     a.in_scale = L.fp8_in ? net->act_scale[l] : 1.0f;
     a.out_qinv = L.fp8_out ? 1.0f / net->act_scale[l + 1] : 1.0f;
+    a.part = reinterpret_cast<float*>(net->ws + P.off_part);
     int64_t out_cs = 0;
     if (last) {
       a.out = reinterpret_cast<uint8_t*>(desc);
