@@ -584,6 +584,11 @@ static int kabsch3f(const float* x, const float* y, const int32_t s[3], float R[
   return 0;
 }
 
+/* Exported for the tests: the FP32 trial fit on the listed three correspondences. */
+int orc_kabsch3f(const float* x, const float* y, const int32_t s[3], float R[9], float t[3]) {
+  return kabsch3f(x, y, s, R, t);
+}
+
 /* Inlier count of model (R,t) in float: |x - (R y + t)|^2 < thr^2, strict as
  * euc3Ddist in ransacfitRt.m:51-61. */
 static int count_inliers(const float* x, const float* y, int m, const float Rf[9], const float tf[3], float thr2,

@@ -79,6 +79,7 @@ def lib():
             "orc_nn": (None, [P, i32, P, i32, i32, P]),
             "orc_mutual_nn": (i32, [P, i32, P, i32, i32, P, P, P]),
             "orc_kabsch": (i32, [P, P, P, i32, P, P]),
+            "orc_kabsch3f": (i32, [P, P, P, P, P]),
             "orc_ransac_trial": (i32, [P, P, i32, u64, ctypes.c_uint32, f32, P, P]),
             "orc_ransac": (i32, [P, P, i32, u64, i32, f32, P, P, P, P]),
             "orc_ransac_adaptive_stop": (i32, [P, i32, i32, i32, P]),
@@ -326,6 +327,18 @@ def ransac_sample(seed: int, h: int, m: int):
     out = np.zeros(3, np.int32)
     lib().orc_ransac_sample(seed, h, m, _p(out))
     return out
+
+
+def kabsch3f(x: np.ndarray, y: np.ndarray, idx):
+    """RANSAC's FP32 three-point fit (x = R y + t) on correspondences idx[0..2]."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    idx = np.ascontiguousarray(idx, np.int32)
+    R = np.zeros(9, np.float32)
+    t = np.zeros(3, np.float32)
+    if lib().orc_kabsch3f(_p(x), _p(y), _p(idx), _p(R), _p(t)) != 0:
+        raise ValueError("degenerate fit")
+    return R.reshape(3, 3), t
 
 
 def kabsch(x: np.ndarray, y: np.ndarray, idx=None):

@@ -107,6 +107,43 @@ def test_ransac_recovers_transform(oracle):
     assert 10 <= n <= 2000 and c[best] == c[:n].max()
 
 
+def test_fp32_trial_fit_is_kabsch(oracle):
+    """RANSAC's FP32 three-point fit agrees with the FP64 Kabsch fit of the same
+    triple, is a proper rotation, and recovers an exact rigid motion.  The gap
+    grows with the triangle's conditioning (thin triangles: FP32 resolves the
+    second singular direction to ~1e-5 of s0/s1), so it is bounded relative to
+    that; the median gap is ~3e-7."""
+    rng = np.random.default_rng(11)
+    gaps = []
+    for trial in range(300):
+        y = rng.uniform(-2.0, 2.0, (3, 3)).astype(np.float32)
+        a = np.cross(y[1] - y[0], y[2] - y[0])
+        if np.linalg.norm(a) < 0.5:  # skip near-degenerate triangles
+            continue
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        ang = rng.uniform(-np.pi, np.pi)
+        K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+        Rt = np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * K @ K
+        tt = rng.uniform(-1, 1, 3)
+        x = (y.astype(np.float64) @ Rt.T + tt + rng.normal(scale=0.002, size=(3, 3))).astype(np.float32)
+        R32, t32 = oracle.kabsch3f(x, y, [0, 1, 2])
+        R64, t64 = oracle.kabsch(x, y)
+        gap = max(float(np.abs(R32 - R64).max()), float(np.abs(t32 - t64).max()))
+        sv = np.linalg.svd((y - y.mean(0)).T.astype(np.float64) @ (x - x.mean(0)), compute_uv=False)
+        assert gap <= 2e-5 * sv[0] / sv[1] + 1e-5, (gap, sv)
+        gaps.append(gap)
+        assert abs(np.linalg.det(R32.astype(np.float64)) - 1.0) < 1e-5
+        assert np.abs(R32.astype(np.float64) @ R32.T - np.eye(3)).max() < 1e-5
+    assert np.median(gaps) < 2e-6, np.median(gaps)
+    # exact data: the motion itself
+    y = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0.5]], np.float32)
+    R = np.array([[0, -1, 0], [1, 0, 0], [0, 0, 1]], np.float64)
+    x = (y @ R.T + np.array([0.5, -0.25, 1.0])).astype(np.float32)
+    R32, t32 = oracle.kabsch3f(x, y, [0, 1, 2])
+    assert np.abs(R32 - R).max() < 1e-6 and np.abs(t32 - [0.5, -0.25, 1.0]).max() < 1e-6
+
+
 def test_marvin_roundtrip(oracle, tmp_path):
     w = oracle.he_normal_weights(4)
     p = str(tmp_path / "w.marvin")
