@@ -1062,7 +1062,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
 #endif
     const int q = warp & 3;
     const int L = q * 32 + lane;  // TMEM lane = row within the 128-row sub-tile
-    const int64_t D3 = (int64_t)p.D * p.D * p.D;
     const int n0 = half * kDxfNt;
     bool issued = false;  // this lane has bulk stores in flight
     uint32_t j = 0;
