@@ -194,7 +194,10 @@ extern "C" tdm_status tdm_register_pair_host(tdm_pipeline* p, const float* a, in
   const int32_t n[2] = {na, nb};
   for (int f = 0; f < 2; ++f) {
     TDM_CHECK_CUDA(cudaMemcpyAsync(p->pts[f], src[f], (size_t)n[f] * 12, cudaMemcpyHostToDevice, s));
-    tdm_status st = tdm_grid_from_points_host(src[f], n[f], p->cfg.voxel_size, trunc, p->cfg.pad, &g[f]);
+    // the grid from the copied points on the device (the same bits as the host
+    // form): a host pass over 150k points costs ~0.3 ms while the GPU has
+    // nothing queued, the device bounding box ~4 us plus one small readback
+    tdm_status st = tdm_grid_from_points(p->pts[f], n[f], p->cfg.voxel_size, trunc, p->cfg.pad, &g[f], p->grid_ws, s);
     if (st) return st;
     st = fragment_front(p, f, p->pts[f], n[f], g[f], seed + (uint64_t)f, k, p->kp[f],
                         p->patches + (size_t)f * k * 27000, s);
