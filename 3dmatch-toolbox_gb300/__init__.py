@@ -27,7 +27,7 @@ STATUS = {0: "OK", 1: "INVALID_ARG", 2: "IO", 3: "FORMAT", 4: "OOM", 5: "DEVICE"
 
 # Every symbol include/tdm.h declares (checked by the CPU tests).
 EXPORTS = [
-    "tdm_version", "tdm_last_error", "tdm_device_status", "tdm_launch_count",
+    "tdm_version", "tdm_last_error", "tdm_device_status", "tdm_launch_count", "tdm_selftest_wait_timeout",
     "tdm_grid_from_points_host", "tdm_grid_workspace_bytes", "tdm_grid_from_points",
     "tdm_tdf_workspace_bytes", "tdm_tdf",
     "tdm_keypoint_indices", "tdm_keypoints", "tdm_gather",
@@ -121,6 +121,7 @@ def lib():
         "tdm_last_error": (ctypes.c_char_p, []),
         "tdm_device_status": (i32, [P]),
         "tdm_launch_count": (i64, []),
+        "tdm_selftest_wait_timeout": (i32, [ctypes.c_uint32, P, P]),
         "tdm_grid_from_points_host": (i32, [P, i32, f32, f32, i32, G]),
         "tdm_grid_workspace_bytes": (sz, []),
         "tdm_grid_from_points": (i32, [P, i32, f32, f32, i32, G, P, P]),
@@ -216,6 +217,16 @@ def _stream(stream) -> int:
 
 def device_status(stream=None) -> None:
     check(lib().tdm_device_status(_stream(stream)))
+
+
+def selftest_wait_timeout(budget_us: int, device="cuda", stream=None):
+    """Runs the bounded-wait self-test kernel (a wait that nothing satisfies,
+    given up after budget_us); returns its 3 result words.  The device error
+    word is raised: the next device_status() raises TdmError(TIMEOUT)."""
+    import torch
+    out = torch.zeros(3, dtype=torch.int32, device=device)
+    check(lib().tdm_selftest_wait_timeout(budget_us, _ptr(out), _stream(stream)))
+    return out.cpu().tolist()
 
 
 def launch_count() -> int:

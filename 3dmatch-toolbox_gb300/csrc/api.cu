@@ -2,12 +2,15 @@
 // and the voxel-grid geometry of core/demo.cu:97-124.
 #include <atomic>
 #include <cmath>
+#include <map>
+#include <utility>
 #include <cstdio>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "common.cuh"
+#include "internal.h"
 #include "tdf_core.cuh"
 
 namespace tdm {
@@ -47,6 +50,39 @@ int* device_error_word() {
   return words[dev];
 }
 
+int device_sm_count() {
+  static std::mutex mu;
+  static std::vector<int> counts;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)counts.size() <= dev) counts.resize(dev + 1, 0);
+  if (counts[dev] == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 148;
+    counts[dev] = n;
+  }
+  return counts[dev];
+}
+
+// The dynamic shared-memory cap is an attribute of a kernel on one device:
+// each (kernel, device) pair gets it once, from whichever host thread comes
+// first; later calls return the recorded outcome.
+cudaError_t raise_smem_cap(const void* func, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, cudaError_t> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(func, dev);
+  auto it = done.find(key);
+  if (it != done.end()) return it->second;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  done[key] = e;
+  return e;
+}
+
 }  // namespace tdm
 
 using namespace tdm;
@@ -68,6 +104,12 @@ extern "C" tdm_status tdm_device_status(tdm_stream s) {
   TDM_CHECK_CUDA(cudaStreamSynchronize(s));
   const char* what = h == DEV_BAD_INDEX ? "index check failed in a kernel" : "a bounded device wait ran out";
   return fail(h == DEV_BAD_INDEX ? TDM_ERR_DEVICE : TDM_ERR_TIMEOUT, std::string("device error: ") + what);
+}
+
+extern "C" tdm_status tdm_selftest_wait_timeout(uint32_t budget_us, int32_t* out_dev, tdm_stream s) {
+  TDM_REQUIRE(out_dev, "tdm_selftest_wait_timeout: null pointer");
+  TDM_REQUIRE(budget_us >= 1 && budget_us <= 1000000, "tdm_selftest_wait_timeout: budget must be 1 us .. 1 s");
+  return launch_wait_selftest((uint64_t)budget_us * 1000ull, out_dev, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -93,12 +135,15 @@ tdm_status grid_from_minmax(const float mn[3], const float mx[3], float vs, floa
 extern "C" tdm_status tdm_grid_from_points_host(const float* pts, int32_t n, float vs, float trunc, int32_t pad,
                                                 tdm_grid* g) {
   TDM_REQUIRE(pts && g && n > 0, "tdm_grid_from_points_host: null pointer or n <= 0");
-  float mn[3] = {pts[0], pts[1], pts[2]}, mx[3] = {pts[0], pts[1], pts[2]};
+  // Bounds as the device form takes them (fminf/fmaxf from +/-inf): a NaN
+  // coordinate is skipped, so both forms give the same grid for any input.
+  // For finite clouds this is the reference's running min/max from pts[0].
+  float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (int32_t i = 0; i < n; ++i)
     for (int a = 0; a < 3; ++a) {
       float v = pts[3 * (int64_t)i + a];
-      mn[a] = v < mn[a] ? v : mn[a];
-      mx[a] = v > mx[a] ? v : mx[a];
+      mn[a] = std::fmin(mn[a], v);
+      mx[a] = std::fmax(mx[a], v);
     }
   return grid_from_minmax(mn, mx, vs, trunc, pad, g);
 }

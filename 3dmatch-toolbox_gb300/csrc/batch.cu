@@ -197,9 +197,11 @@ __global__ __launch_bounds__(256) void occupancy_kernel(const float* __restrict_
     const int f = find_frag(sb, F, i);
     const FragGeo g = geo[f];
     const float vs = in[f].vs;
-    const int gx = voxel_coord(pts[3 * i], g.origin[0], vs);
-    const int gy = voxel_coord(pts[3 * i + 1], g.origin[1], vs);
-    const int gz = voxel_coord(pts[3 * i + 2], g.origin[2], vs);
+    const float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
+    if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;  // skipped, as by the grid bounds
+    const int gx = voxel_coord(px, g.origin[0], vs);
+    const int gy = voxel_coord(py, g.origin[1], vs);
+    const int gz = voxel_coord(pz, g.origin[2], vs);
     if (gx < 0 || gy < 0 || gz < 0 || gx >= g.dim[0] || gy >= g.dim[1] || gz >= g.dim[2]) continue;
     occ[g.vox_off + ((int64_t)gz * g.dim[1] + gy) * occ_pitch(g.dim[0]) + gx] = 1;
   }

@@ -19,6 +19,11 @@ tdm_status cuda_status(cudaError_t e, const char* what);
 // Per-device error word written by kernels whose bounded waits ran out or
 // whose index checks failed.  Lazily allocated, one int per device.
 int* device_error_word();
+// SM count of the current device (cached per device).
+int device_sm_count();
+// Raises `func`'s dynamic shared-memory cap to `bytes` on the current device,
+// once per (kernel, device); returns the outcome of that first call.
+cudaError_t raise_smem_cap(const void* func, int bytes);
 
 enum DeviceError : int {
   DEV_OK = 0,

@@ -75,7 +75,11 @@ __host__ __device__ constexpr uint32_t tmem_cols_for(int c) {
 
 __device__ __forceinline__ bool aborted(const int* err) { return *reinterpret_cast<const volatile int*>(err) != 0; }
 
-__device__ __forceinline__ bool wait_or_flag(uint32_t bar, uint32_t parity, int* err, int code) {
+// Waits for phase `parity` of `bar`.  Gives up (false) when another role of
+// the kernel has raised the error word, or after budget_ns of wall time, when
+// it raises the word with `code` itself.
+__device__ __forceinline__ bool wait_or_flag(uint32_t bar, uint32_t parity, int* err, int code,
+                                             uint64_t budget_ns = kWaitBudgetNs) {
   if (ptx::mbar_try_wait(bar, parity)) return true;
   uint64_t t0 = ptx::globaltimer_ns();
   uint32_t spins = 0;
@@ -83,7 +87,7 @@ __device__ __forceinline__ bool wait_or_flag(uint32_t bar, uint32_t parity, int*
     if (ptx::mbar_try_wait(bar, parity)) return true;
     if ((++spins & 255u) == 0) {
       if (aborted(err)) return false;
-      if (ptx::globaltimer_ns() - t0 > kWaitBudgetNs) {
+      if (ptx::globaltimer_ns() - t0 > budget_ns) {
         atomicCAS(err, 0, code);
         return false;
       }
@@ -1475,15 +1479,7 @@ size_t smem_bytes(const TcLayer& L) {
   return grid_a_stages(L) * a_stage_bytes(L) + (size_t)weight_stages(L) * L.nt * 128 + kSmemReserve;
 }
 
-int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
-  }
-  return n;
-}
+int sm_count() { return device_sm_count(); }
 
 template <int NT, int MSUB, bool FP8_IN, bool FP8_OUT>
 tdm_status launch_t(const KParams& kp, size_t smem, cudaStream_t s) {
@@ -1491,13 +1487,9 @@ tdm_status launch_t(const KParams& kp, size_t smem, cudaStream_t s) {
   // Every tcgen05 CTA takes more than half an SM's shared memory, so two
   // TMEM-allocating CTAs never share an SM.
   size_t req = std::max<size_t>(smem, 120 * 1024);
-  // The attribute is a cap shared by every launch of this instantiation (from
-  // any host thread): raise it once to the full budget.
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
-  std::call_once(once, [&] {
-    attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  });
+  // The attribute is a per-device cap shared by every launch of this
+  // instantiation: raise it to the full budget once per device.
+  cudaError_t attr_err = raise_smem_cap(reinterpret_cast<const void*>(kern), (int)kSmemLimit);
   if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_kernel)");
   int64_t grid = std::min<int64_t>(kp.total_tiles, sm_count());
   kern<<<(unsigned)std::max<int64_t>(grid, 1), kThreads, req, s>>>(kp);
@@ -1509,16 +1501,58 @@ template <int NT, int MSUB, bool FP8, bool XRUN, bool WT = false>
 tdm_status launch_g(const KParams& kp, size_t smem, cudaStream_t s) {
   auto kern = tc_conv_gather_kernel<NT, MSUB, FP8, XRUN, WT>;
   size_t req = std::max<size_t>(smem, 120 * 1024);
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
-  std::call_once(once, [&] {
-    attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  });
+  cudaError_t attr_err = raise_smem_cap(reinterpret_cast<const void*>(kern), (int)kSmemLimit);
   if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_gather_kernel)");
   int64_t grid = std::min<int64_t>(kp.total_tiles, sm_count());
   kern<<<(unsigned)std::max<int64_t>(grid, 1), kGThreads, req, s>>>(kp);
   TDM_CHECK_LAUNCH("tc_conv_gather_kernel");
   return TDM_OK;
+}
+
+// Self-test of the bounded-wait path the tcgen05 kernels share.  One CTA of
+// 64 threads allocates 32 TMEM columns the way the MMA warp does, lands one
+// 64-byte bulk copy on barrier `full` (that wait completes), then waits on
+// barrier `never`, on which nothing ever arrives.  That wait gives up after
+// budget_ns and raises the device error word (DEV_TIMEOUT_MMA); the CTA then
+// frees its TMEM and returns like a timed-out conv kernel.  out[0] = the copy
+// landed, out[1] = the second wait ran out, out[2] = first copied word.
+__device__ __align__(16) uint32_t g_selftest_src[16] = {0x5E1F7E57u, 1, 2, 3, 4, 5, 6, 7,
+                                                        8, 9, 10, 11, 12, 13, 14, 15};
+
+__global__ void __launch_bounds__(64, 1) wait_selftest_kernel(uint64_t budget_ns, int* err, int32_t* out) {
+  __shared__ __align__(16) uint32_t buf[16];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ uint32_t tmem_slot;
+  const int warp = threadIdx.x >> 5;
+  const uint32_t full = ptx::smem_u32(&bars[0]), never = ptx::smem_u32(&bars[1]);
+  if (threadIdx.x == 0) {
+    ptx::mbar_init(full, 1);
+    ptx::mbar_init(never, 1);
+    ptx::fence_barrier_init();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(ptx::smem_u32(&tmem_slot), 32);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  if (threadIdx.x == 0) {
+    ptx::mbar_arrive_expect_tx(full, sizeof(buf));
+    ptx::bulk_g2s(ptx::smem_u32(buf), g_selftest_src, sizeof(buf), full);
+    const bool copied = wait_or_flag(full, 0, err, DEV_TIMEOUT_PRODUCER, budget_ns);
+    const bool timed_out = !wait_or_flag(never, 0, err, DEV_TIMEOUT_MMA, budget_ns);
+    out[0] = copied ? 1 : 0;
+    out[1] = timed_out ? 1 : 0;
+    out[2] = copied ? (int32_t)buf[0] : 0;
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, 32);
+  }
 }
 
 // (N tile, M sub-tiles) shapes the gathered-row kernel is built for
@@ -1530,11 +1564,7 @@ template <int MSUB, bool FP8_OUT, bool XPOOL>
 tdm_status launch_dxf(const KParams& kp, size_t smem, cudaStream_t s) {
   auto kern = tc_conv_dxf_kernel<MSUB, FP8_OUT, XPOOL>;
   size_t req = std::max<size_t>(smem, 120 * 1024);
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
-  std::call_once(once, [&] {
-    attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  });
+  cudaError_t attr_err = raise_smem_cap(reinterpret_cast<const void*>(kern), (int)kSmemLimit);
   if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_dxf_kernel)");
   // an even grid keeps every CTA on one half of the output channels
   int64_t grid = std::min<int64_t>(kp.total_tiles, sm_count() & ~1);
@@ -1563,15 +1593,19 @@ tdm_status launch_conv1_tc(const float* patches, int B, const TcLayer& L, uint8_
   if (!p.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
   if (p.rows == 0) return TDM_OK;
   const size_t smem = kC1W + kC1NSA * kC1Stage + 256;
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
-  std::call_once(once, [&] {
-    attr_err = cudaFuncSetAttribute(tc_conv1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  });
+  cudaError_t attr_err = raise_smem_cap(reinterpret_cast<const void*>(tc_conv1_kernel), (int)kSmemLimit);
   if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv1_kernel)");
   const int64_t grid = std::min<int64_t>(p.tiles, sm_count());
   tc_conv1_kernel<<<(unsigned)grid, kC1Threads, std::max<size_t>(smem, 120 * 1024), s>>>(p);
   TDM_CHECK_LAUNCH("tc_conv1_kernel");
+  return TDM_OK;
+}
+
+tdm_status launch_wait_selftest(uint64_t budget_ns, int32_t* out, cudaStream_t s) {
+  int* err = device_error_word();
+  if (!err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
+  wait_selftest_kernel<<<1, 64, 0, s>>>(budget_ns, err, out);
+  TDM_CHECK_LAUNCH("wait_selftest_kernel");
   return TDM_OK;
 }
 

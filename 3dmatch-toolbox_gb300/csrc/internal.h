@@ -89,6 +89,9 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s);
 // layer's packed weights and bias); writes conv2's chunk-planar BF16 input.
 tdm_status launch_conv1_tc(const float* patches, int B, const TcLayer& L, uint8_t* out, int64_t out_cs,
                            cudaStream_t s);
+// One-CTA kernel that runs the tcgen05 kernels' bounded wait into its time
+// limit on purpose (out: 3 int32 on the device); raises the error word.
+tdm_status launch_wait_selftest(uint64_t budget_ns, int32_t* out, cudaStream_t s);
 // Whether layer L's (nt, msub) tile fits the shared-memory plan and TMEM.
 bool tc_layer_fits(const TcLayer& L);
 // Packs Marvin-layout weights [cout][cin][taps] (taps = nz*nyx, or the GEMM

@@ -225,14 +225,9 @@ __global__ void pairs_to_points_kernel(const float* __restrict__ ka, const float
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Raises trials_kernel's dynamic shared-memory cap once (any host thread).
+// Raises trials_kernel's dynamic shared-memory cap (once per device).
 cudaError_t trials_smem_cap() {
-  static std::once_flag once;
-  static cudaError_t err = cudaSuccess;
-  std::call_once(once, [] {
-    err = cudaFuncSetAttribute(trials_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * 4096 * 4);
-  });
-  return err;
+  return raise_smem_cap(reinterpret_cast<const void*>(trials_kernel), 6 * 4096 * 4);
 }
 
 }  // namespace

@@ -68,6 +68,7 @@ __global__ __launch_bounds__(256) void occupancy_kernel(const float* __restrict_
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float px = pts[3 * (int64_t)i], py = pts[3 * (int64_t)i + 1], pz = pts[3 * (int64_t)i + 2];
+  if (!(isfinite(px) && isfinite(py) && isfinite(pz))) return;  // skipped, as by the grid bounds
   int gx = voxel_coord(px, ox, vs), gy = voxel_coord(py, oy, vs), gz = voxel_coord(pz, oz, vs);
   if (gx < 0 || gy < 0 || gz < 0 || gx >= dx || gy >= dy || gz >= dz) return;
   occ[((int64_t)gz * dy + gy) * occ_pitch(dx) + gx] = 1;
@@ -102,16 +103,7 @@ __global__ __launch_bounds__(kZThreads) void tdf_z_kernel(const uint8_t* __restr
   }
 }
 
-int z_blocks() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 148;
-    n = sms * 16;
-  }
-  return n;
-}
+int z_blocks() { return tdm::device_sm_count() * 16; }
 
 // The reference decodes voxel_idx through float32 (core/demo.cu:32-34); above
 // 2^24 that lands on a different (x,y,z).  mode 1 evaluates its expressions

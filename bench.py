@@ -152,29 +152,33 @@ class Clocks:
 # --------------------------------------------------------------------------
 # CPU baseline: the oracle's restated reference loops on a bounded sample
 # --------------------------------------------------------------------------
-def cpu_sample(pair, k, ransac_iters, scale):
-    """Times one bounded sample of the pair workload on the host cores and
-    extrapolates to a whole pair.  scale 1.0 ~ 10-20 s of CPU work."""
+MARVIN_BATCH = 50  # patches per net forward in core/demo.cu:195 (one Marvin batch)
+
+
+def cpu_sample(pair, k, ransac_iters, ransac_sample_iters=20_000):
+    """Times one bounded sample of the pair workload on all host cores with the
+    oracle's restated reference loops (OpenMP C) and extrapolates it linearly
+    to a whole pair.  The sample: the whole-grid TDF of fragment A (one of the
+    pair's two grids), one Marvin batch of 50 of its 30^3 patches through the
+    net (2k per pair), the full k x k mutual NN, and `ransac_sample_iters` of
+    the pair's RANSAC trials.  Returns (pairs/s extrapolated, seconds the
+    sample took, fraction of a pair's work the sample is, description, parts)."""
     from oracle import oracle as O
     O.set_threads(os.cpu_count() or 1)
     a, b, _ = pair
-    t_tdf = 0.0
-    for pts in (a, b):
-        dim, origin = O.grid_setup(pts)
-        occ = O.occupancy(pts, dim, origin, 0.01)
-        V = int(np.prod(dim.astype(np.int64)))
-        nv = int(2_000_000 * scale)
-        v0 = V // 3
-        t0 = time.perf_counter()
-        O.tdf(occ, dim, 0.01, np.float32(0.01) * np.float32(5), 0, v0, v0 + nv)
-        t_tdf += (time.perf_counter() - t0) * V / nv
+    dim, origin = O.grid_setup(a)
+    occ = O.occupancy(a, dim, origin, 0.01)
+    t0 = time.perf_counter()
+    tdf = O.tdf(occ, dim, 0.01, np.float32(0.01) * np.float32(5))
+    t_tdf = time.perf_counter() - t0
+    idx = O.keypoint_indices(1, a.shape[0], MARVIN_BATCH)
+    _, kg = O.keypoints(a, idx, origin, 0.01)
+    patches = O.gather(tdf, dim, kg)
     w = O.he_normal_weights(1)
-    npatch = max(1, int(8 * scale))
-    rng = np.random.default_rng(0)
-    patches = (rng.random((npatch, 27000)) * (rng.random((npatch, 27000)) < 0.15)).astype(np.float32)
     t0 = time.perf_counter()
     O.net_forward(patches, w)
-    t_net = (time.perf_counter() - t0) * (2 * k) / npatch
+    t_net = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
     da = rng.normal(size=(k, 512)).astype(np.float32)
     db = rng.normal(size=(k, 512)).astype(np.float32)
     t0 = time.perf_counter()
@@ -183,16 +187,19 @@ def cpu_sample(pair, k, ransac_iters, scale):
     m = 300
     x = rng.uniform(-1, 1, (m, 3)).astype(np.float32)
     y = rng.uniform(-1, 1, (m, 3)).astype(np.float32)
-    it = max(1000, int(ransac_iters * 0.2 * scale))
+    it = min(ransac_iters, ransac_sample_iters)
     t0 = time.perf_counter()
     O.ransac(x, y, 1, it, 0.05)
-    t_ransac = (time.perf_counter() - t0) * ransac_iters / it
-    t_pair = t_tdf + t_net + t_mnn + t_ransac
-    sample = ("TDF %d voxels x2 fragments (scaled to full grids), net %d patches (scaled to %d), "
-              "MNN %dx%d, RANSAC %d trials (scaled to %d), m=%d" % (int(2_000_000 * scale), npatch, 2 * k, k, k,
-                                                                    it, ransac_iters, m))
-    parts = {"tdf_s": t_tdf, "net_s": t_net, "mnn_s": t_mnn, "ransac_s": t_ransac}
-    return 1.0 / t_pair, sample, parts
+    t_ransac = time.perf_counter() - t0
+    sample_s = t_tdf + t_net + t_mnn + t_ransac
+    # whole pair: two grids, 2k patches, one MNN, all RANSAC trials
+    parts = {"tdf_s": 2 * t_tdf, "net_s": t_net * (2 * k) / MARVIN_BATCH, "mnn_s": t_mnn,
+             "ransac_s": t_ransac * ransac_iters / it}
+    t_pair = sum(parts.values())
+    sample = ("whole-grid TDF of one fragment (%d voxels; x2 per pair), net on one Marvin batch of %d gathered "
+              "patches (x%.0f per pair), MNN %dx%d, RANSAC %d of %d trials (m=%d); extrapolated linearly"
+              % (int(np.prod(dim.astype(np.int64))), MARVIN_BATCH, 2 * k / MARVIN_BATCH, k, k, it, ransac_iters, m))
+    return 1.0 / t_pair, sample_s, sample_s / t_pair, sample, parts
 
 
 def run_reference(args, rank, world):
@@ -202,26 +209,31 @@ def run_reference(args, rank, world):
     ge.load()
     from tdm_gb300 import synth
     pair = synth.fragment_pair(20260000, n_points=args.points)
-    scale = 0.15
     for _ in range(args.warmup):
-        cpu_sample(pair, args.keypoints, args.ransac_iters, scale)
-    vals = []
+        cpu_sample(pair, args.keypoints, args.ransac_iters)
+    rates, secs, fracs = [], [], []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, sample, parts = cpu_sample(pair, args.keypoints, args.ransac_iters, scale)
-        vals.append(v)
+        v, sec, frac, sample, parts = cpu_sample(pair, args.keypoints, args.ransac_iters)
+        rates.append(v)
+        secs.append(sec)
+        fracs.append(frac)
     wall = time.perf_counter() - t0
-    value = float(np.mean(vals))
+    # a step is one sample: ms_per_step is its measured time, and the rate is
+    # the pair fraction the steps covered over the time they took
+    value = float(np.sum(fracs) / np.sum(secs))
     cores = os.cpu_count() or 1
     line = {
         "impl": "reference", "metric": "pair registrations/s", "value": value, "unit": "pairs/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * float(np.mean(secs)), "pair_fraction_per_step": float(np.mean(fracs)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "demo pipeline pair: 2 x %d-point synthetic room fragments, 1 cm TDF, %d keypoints "
                                "per fragment, 30^3 patches, 9-layer net, mutual NN, RANSAC %d trials"
                                % (args.points, args.keypoints, args.ransac_iters)},
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
-                         "sample": sample + "; wall %.1fs for %d steps" % (wall, args.steps)},
+                         "sample": sample + "; one sample per step, wall %.1fs for %d steps" % (wall, args.steps),
+                         "parts_s_per_pair": {kk: round(vv, 3) for kk, vv in parts.items()}},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU restatement of the reference loops (oracle/oracle.c, OpenMP); the reference's own "
                 "demo.cu needs OpenCV and cuDNN and MATLAB for matching, so it is not built here",
@@ -450,10 +462,12 @@ def run_ours(args, rank, world, local):
     if conv2_n > 0:
         flop = CONV2_FLOP_PER_PATCH * 2 * k
         achieved = flop / (conv2_ms / conv2_n / 1000.0) / 1e12
-        peak = peaks["bf16_tflops_sustained"] if prec == "bf16" else None
+        # burst peak: conv2 runs inside a ~14 ms step at full clocks, not a
+        # seconds-long loop under the power cap
+        peak = peaks["bf16_tflops"] if prec == "bf16" else None
         roof = {"kernel": "tc_conv_dxf_kernel<2,false> (conv2, %d patches per launch)" % (2 * k),
                 "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": (achieved / peak) if peak else None, "peak_source": peak_kind + " bf16 sustained",
+                "frac": (achieved / peak) if peak else None, "peak_source": peak_kind + " bf16 burst",
                 "traffic": profile_traffic("conv2_dxf_bf16"),
                 "ms_per_launch": conv2_ms / conv2_n, "share_of_step": (conv2_ms / args.steps) / ms_step}
     layer_ms = {name: round(v[0] / max(1, v[1]), 4) for name, v in lt.items() if v[1]}
@@ -461,9 +475,10 @@ def run_ours(args, rank, world, local):
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            v, sample, parts = cpu_sample(pairs[0], k, args.ransac_iters, 4.0)
+            v, sec, _, sample, parts = cpu_sample(pairs[0], k, args.ransac_iters)
             cpu = {"value": v, "unit": "pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
-                   "sample": sample, "parts_s_per_pair": {kk: round(vv, 3) for kk, vv in parts.items()}}
+                   "sample": sample + " (%.1f s)" % sec,
+                   "parts_s_per_pair": {kk: round(vv, 3) for kk, vv in parts.items()}}
         out = {
             "metric": "pair registrations/s", "value": value, "unit": "pairs/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,

@@ -65,9 +65,24 @@ tdm_status tdm_device_status(tdm_stream s);
 /* Number of kernels this library has launched in this process (diagnostics;
  * the reference has no counterpart). */
 int64_t tdm_launch_count(void);
+/* Self-test of the failure path (no reference counterpart; the reference's
+ * FatalError exits the process, core/marvin.hpp:132-138).  Launches one small
+ * kernel that makes the bounded mbarrier wait of the tcgen05 kernels run out
+ * after budget_us (1 .. 1,000,000): it allocates tensor memory, completes one
+ * bulk copy, waits on a barrier nothing arrives on, gives up, raises the
+ * device error word, frees its tensor memory and returns.  out_dev: 3 int32
+ * {copy landed, wait ran out, first copied word (0x5E1F7E57)}.  The next
+ * tdm_device_status reports TDM_ERR_TIMEOUT and clears the word; the context
+ * stays usable. */
+tdm_status tdm_selftest_wait_timeout(uint32_t budget_us, int32_t* out_dev, tdm_stream s);
 
 /* ---- grid + TDF: replaces core/demo.cu:97-158 (ComputeTDF) ---------------- */
-/* Grid of core/demo.cu:97-124 from host points (float ops as the reference). */
+/* Grid of core/demo.cu:97-124 from host points (float ops as the reference).
+ * Point clouds are expected to be finite.  A NaN coordinate is skipped by the
+ * bounds (fminf/fmaxf from +/-inf, as the device form), and a point with any
+ * non-finite coordinate is skipped by the occupancy scatter, so the host and
+ * device forms give the same grid for any input; an infinite bound is
+ * TDM_ERR_INVALID_ARG. */
 tdm_status tdm_grid_from_points_host(const float* pts_host, int32_t n, float voxel_size, float trunc_margin,
                                      int32_t pad, tdm_grid* grid_out);
 /* Same from device points: min/max reduced on the device, then read back

@@ -101,13 +101,14 @@ void orc_grid_setup(const float* pts, int n, float voxel_size, int pad, int dim[
 }
 
 /* occ[z*dy*dx + y*dx + x] = 1 with x = round((p - o) / vs).  Points that land
- * outside the grid are skipped (the reference has no check; with its padding
- * they cannot occur). */
+ * outside the grid, or have a non-finite coordinate, are skipped (the
+ * reference has no check; with its padding and finite clouds neither occurs). */
 void orc_occupancy(const float* pts, int n, const int dim[3], const float origin[3], float vs, uint8_t* occ) {
   size_t V = (size_t)dim[0] * dim[1] * dim[2];
   memset(occ, 0, V);
   for (int i = 0; i < n; ++i) {
     int g[3];
+    if (!(isfinite(pts[3 * i]) && isfinite(pts[3 * i + 1]) && isfinite(pts[3 * i + 2]))) continue;
     for (int a = 0; a < 3; ++a) g[a] = (int)roundf((pts[3 * i + a] - origin[a]) / vs);
     if (g[0] < 0 || g[1] < 0 || g[2] < 0 || g[0] >= dim[0] || g[1] >= dim[1] || g[2] >= dim[2]) continue;
     occ[(size_t)g[2] * dim[1] * dim[0] + (size_t)g[1] * dim[0] + g[0]] = 1;

@@ -289,6 +289,103 @@ def net_forward(patches: np.ndarray, weights: dict, use_feat: bool = True, f64: 
     return out
 
 
+def round_bf16(x) -> np.ndarray:
+    """Round to bfloat16 (nearest, ties to even), returned as float64."""
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(x, np.float32))
+    return t.to(torch.bfloat16).to(torch.float64).numpy()
+
+
+def round_e4m3(x) -> np.ndarray:
+    """Round to FP8 E4M3 (nearest, ties to even, saturating at +-448, as the
+    cvt.rn.satfinite conversion), returned as float64."""
+    import torch
+    t = torch.from_numpy(np.clip(np.asarray(x, np.float32), -448.0, 448.0))
+    return t.to(torch.float8_e4m3fn).to(torch.float64).numpy()
+
+
+def net_forward_quantized(patches: np.ndarray, weights: dict, fp8_layers=(), act_scales=None,
+                          want=None):
+    """Float64 forward of the net with the operand and storage rounding of the
+    tensor-core forms, for checking those kernels and for choosing layers.
+
+    Every layer multiplies BF16 operands (patches and weights rounded to
+    BF16) and stores its ReLU output rounded to BF16, except the layers
+    listed in `fp8_layers` (indices 2..7 = conv3..conv8): their input is the
+    E4M3 code of x / act_scales[l], their weights the E4M3 code of
+    w / s_k with s_k = max|w_k| / 448 per output channel (float32), and the
+    sum is scaled back by act_scales[l] * s_k before the bias and ReLU.  The
+    layer before an E4M3 layer stores E4M3 codes of its output /
+    act_scales[l] (conv2's go through the 2^3 max-pool as codes).  Sums are
+    exact float64 (the GPU accumulates in FP32).  `want` names responses to
+    return beside the descriptors ("conv1".."conv8", "pool1", "feat", as
+    float64 channels-last values); returns desc or (desc, responses)."""
+    fp8 = set(int(l) for l in fp8_layers)
+    assert fp8 <= set(range(2, 8)), "E4M3 layers are conv3..conv8 (2..7)"
+    if fp8:
+        assert act_scales is not None
+    L = lib()
+    x = round_bf16(np.ascontiguousarray(patches, np.float32).reshape(-1, 30, 30, 30, 1))
+    B = x.shape[0]
+    D, C = 30, 1
+    resp = {}
+    in_scale = 1.0
+    for l, name in enumerate(NET_LAYERS):
+        K, ks = NET_COUT[l], NET_KS[l]
+        Do = D - ks + 1
+        w = np.ascontiguousarray(weights[name + ".weight"], np.float32).reshape(K, -1)
+        bias = np.ascontiguousarray(weights[name + ".bias"], np.float32).reshape(-1).astype(np.float64)
+        if l in fp8:
+            s_w = (np.abs(w).max(axis=1) / np.float32(448.0)).astype(np.float32)
+            s_w[s_w == 0] = 1.0
+            wq = round_e4m3(w / s_w[:, None]).astype(np.float32)
+            scale = (np.float32(in_scale) * s_w).astype(np.float32).astype(np.float64)
+        else:
+            wq = round_bf16(w).astype(np.float32)
+            scale = np.ones(K)
+        # conv8 reads conv7's output as one 27*512 GEMM row per patch: the same sums
+        y = np.zeros((B, Do, Do, Do, K))
+        zb = np.zeros(K, np.float32)
+        L.orc_conv3d_f64(_p(np.ascontiguousarray(x)), B, D, C, _p(np.ascontiguousarray(wq)), _p(zb), K, ks, 0,
+                         _p(y))
+        v = y * scale + bias
+        if l < 8:
+            v = np.maximum(v, 0.0)
+        D, C = Do, K
+        nxt = l + 1 if l != 1 else 2  # conv2 feeds the pool, whose output is conv3's input
+        if l == 8:
+            x, in_scale = v, 1.0
+        elif nxt in fp8:
+            qinv = np.float32(1.0) / np.float32(act_scales[nxt])
+            x = round_e4m3(v.astype(np.float32) * qinv)
+            in_scale = float(act_scales[nxt])
+        else:
+            x, in_scale = round_bf16(v), 1.0
+        if want and name in want:
+            resp[name] = x * in_scale  # stored values (E4M3 codes times their scale)
+        if l == 1:
+            Dp = D // 2
+            z = np.zeros((B, Dp, Dp, Dp, C))
+            L.orc_pool_f64(_p(np.ascontiguousarray(x)), B, D, C, _p(z))
+            x, D = z, Dp
+            if want and "pool1" in want:
+                resp["pool1"] = x * in_scale
+    desc = x.reshape(B, 512)
+    return (desc, resp) if want else desc
+
+
+def fp8_act_scales(patches: np.ndarray, weights: dict) -> np.ndarray:
+    """The E4M3 activation scales the FP8 form calibrates: for l = 2..7 the
+    largest value of layer l-1's BF16-form response (conv2..conv7) over the
+    calibration patches, divided by 448; index l = the layer that reads it."""
+    _, r = net_forward_quantized(patches, weights, want=["conv2", "conv3", "conv4", "conv5", "conv6", "conv7"])
+    sc = np.ones(9, np.float32)
+    for l, name in zip(range(2, 8), ["conv2", "conv3", "conv4", "conv5", "conv6", "conv7"]):
+        m = np.float32(r[name].max())
+        sc[l] = (m if m > 0 else np.float32(1.0)) / np.float32(448.0)
+    return sc
+
+
 # --------------------------------------------------------------------------
 # Matching and registration
 # --------------------------------------------------------------------------

@@ -7,7 +7,9 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 
-REFERENCE = "/root/reference"
+# Root of the reference tree (read only); tests that need its files skip when
+# it is absent.  TDM_REFERENCE_ROOT overrides the default mount point.
+REFERENCE = os.environ.get("TDM_REFERENCE_ROOT", "/root/reference")
 
 
 def pytest_configure(config):

@@ -2,6 +2,7 @@
 
 Run in a container where the reference tree is mounted (it is read only):
     python tests/golden/make_golden.py [reference_root]
+(default: $TDM_REFERENCE_ROOT, else /root/reference)
 
 Writes, next to this script:
   sampledata.npz   P1h, P2h (4x441) and T (4x4) of
@@ -26,7 +27,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from oracle import oracle as O  # noqa: E402
 
 
-def main(ref="/root/reference"):
+def main(ref=os.environ.get("TDM_REFERENCE_ROOT", "/root/reference")):
     d = scipy.io.loadmat(os.path.join(ref, "core/external/estimateRigidTransform/sampleData.mat"))
     np.savez_compressed(os.path.join(HERE, "sampledata.npz"), P1h=d["P1h"], P2h=d["P2h"], T=d["T"])
     clouds = {}

@@ -86,3 +86,21 @@ def test_seeded_weights_file(built, tdm, oracle, tmp_path):
         assert np.abs(w[n + ".bias"]).max() <= 0.05
     tdm.write_seeded_weights(str(tmp_path / "w2.marvin"), 7)
     assert open(p, "rb").read() == open(str(tmp_path / "w2.marvin"), "rb").read()
+
+
+def test_grid_host_skips_nan_like_the_device_form(built, tdm):
+    """The host bounds skip a NaN coordinate (fminf/fmaxf from +/-inf), the
+    way the device min/max reduction does, even on the first point; an
+    infinite coordinate is rejected."""
+    rng = np.random.default_rng(1)
+    pts = rng.uniform(-1, 2, (2000, 3)).astype(np.float32)
+    bad = np.concatenate([np.array([[np.nan, 5.0, np.nan]], np.float32), pts])
+    g, g_fin = tdm.grid_from_points_host(bad), tdm.grid_from_points_host(pts)
+    # the NaN row's finite y = 5.0 widens the y extent, as on the device
+    both = np.concatenate([np.array([[pts[0, 0], 5.0, pts[0, 2]]], np.float32), pts])
+    g_both = tdm.grid_from_points_host(both)
+    assert tuple(g.dim) == tuple(g_both.dim) and tuple(g.origin) == tuple(g_both.origin)
+    assert g.dim[0] == g_fin.dim[0] and g.dim[2] == g_fin.dim[2]
+    inf = np.concatenate([np.array([[np.inf, 0.0, 0.0]], np.float32), pts])
+    st = built.tdm_grid_from_points_host(inf.ctypes.data, inf.shape[0], 0.01, 0.05, 15, ctypes.byref(tdm.Grid()))
+    assert st == 1

@@ -119,3 +119,27 @@ def test_tdf_exact_against_oracle(tdm, oracle, cuda, scene):
     want = oracle.tdf_exact(pts, list(g.dim), list(g.origin), g.voxel_size, g.trunc_margin)
     assert np.abs(got - want).max() <= 1e-6
     assert (want > 0).sum() > 1000  # the surface band is covered
+
+
+def test_nonfinite_points_are_skipped_by_both_grid_forms(tdm, oracle, cuda, small):
+    """A cloud whose first point has a NaN coordinate (and one with an
+    infinite one) gets, from the host and the device forms alike, the grid and
+    the TDF of its finite points: the bounds skip NaN and the occupancy
+    scatter skips any non-finite point."""
+    import torch
+    finite = small[:5000]
+    bad = np.concatenate([np.array([[np.nan, np.nan, np.nan], [0.3, np.inf, 0.1]], np.float32), finite])
+    # the infinite coordinate would make an infinite bound: keep the NaN row
+    # for the grid and check the occupancy with both rows
+    nan_only = bad[[0] + list(range(2, bad.shape[0]))]
+    g_host = tdm.grid_from_points_host(nan_only)
+    g_dev = tdm.grid_from_points(torch.from_numpy(nan_only).to(cuda))
+    g_fin = tdm.grid_from_points_host(finite)
+    assert tuple(g_host.dim) == tuple(g_dev.dim) == tuple(g_fin.dim)
+    assert tuple(g_host.origin) == tuple(g_dev.origin) == tuple(g_fin.origin)
+    got = tdm.tdf(torch.from_numpy(bad).to(cuda), g_fin).cpu().numpy()
+    dim, origin, occ = _occ(oracle, finite)
+    assert np.array_equal(got, oracle.tdf(occ, dim, VS, TRUNC))
+    with pytest.raises(RuntimeError):
+        tdm.grid_from_points(torch.from_numpy(bad).to(cuda))
+    tdm.device_status()
