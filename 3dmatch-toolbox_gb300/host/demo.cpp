@@ -16,6 +16,8 @@
 //   --precision fp32|bf16  net precision (fp32 = the reference's arithmetic)
 //   --tdf-out              also write tdf.bin (the commented writer at :257-274)
 //   --ref-compat float|fma reproduce the reference's float32 voxel-index decode
+//   --info                 stop after reading the cloud and setting up the grid
+//                          (prints the count, first/last point and grid; no GPU)
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -58,13 +60,13 @@ bool write_floats(std::ofstream& f, const float* v, size_t n) {
 int main(int argc, char** argv) {
   if (argc < 3) {
     std::cerr << "usage: demo <cloud.ply> <out_prefix> [--weights PATH] [--seeded-weights SEED] [--keypoints K]"
-                 " [--seed S] [--precision fp32|bf16] [--tdf-out] [--ref-compat float|fma]"
+                 " [--seed S] [--precision fp32|bf16] [--tdf-out] [--ref-compat float|fma] [--info]"
               << std::endl;
     return 2;
   }
   std::string cloud = argv[1], prefix = argv[2];
   std::string weights = "3dmatch-weights-snapshot-137000.marvin";
-  bool seeded = false, tdf_out = false;
+  bool seeded = false, tdf_out = false, info = false;
   uint64_t wseed = 0, seed = std::random_device{}();
   int k = 50 * 10;
   tdm_precision prec = TDM_FP32;
@@ -78,6 +80,7 @@ int main(int argc, char** argv) {
     else if (a == "--seed") seed = std::strtoull(next().c_str(), nullptr, 10);
     else if (a == "--precision") { std::string p = next(); prec = p == "bf16" ? TDM_BF16 : TDM_FP32; }
     else if (a == "--tdf-out") tdf_out = true;
+    else if (a == "--info") info = true;
     else if (a == "--ref-compat") { std::string m = next(); mode = m == "fma" ? TDM_TDF_REFCOMPAT_FMA : TDM_TDF_REFCOMPAT_FLOAT; }
     else { std::cerr << "unknown option " << a << std::endl; return 2; }
   }
@@ -114,6 +117,14 @@ int main(int argc, char** argv) {
   tdm_grid g;
   if (!ok(tdm_grid_from_points_host(pts.data(), num_pts, voxel_size, trunc_margin, 15, &g), "grid")) return 1;
   std::cout << "Size of TDF voxel grid: " << g.dim[0] << " x " << g.dim[1] << " x " << g.dim[2] << std::endl;
+  if (info) {
+    const size_t last = (size_t)(num_pts - 1) * 3;
+    std::printf("points %d first %.9g %.9g %.9g last %.9g %.9g %.9g\n", num_pts, pts[0], pts[1], pts[2], pts[last],
+                pts[last + 1], pts[last + 2]);
+    std::printf("grid %d %d %d origin %.9g %.9g %.9g\n", g.dim[0], g.dim[1], g.dim[2], g.origin[0], g.origin[1],
+                g.origin[2]);
+    return 0;
+  }
   std::cout << "Computing TDF voxel grid..." << std::endl;
   const size_t V = (size_t)g.dim[0] * g.dim[1] * g.dim[2];
   DevBuf<float> d_pts(pts.size()), d_tdf(V), d_kp((size_t)k * 3), d_patch((size_t)k * 27000), d_desc((size_t)k * 512);

@@ -41,6 +41,33 @@ def test_missing_vertex_count_exits_zero(tmp_path):
     assert not (tmp_path / "out.keypts.bin").exists()
 
 
+def test_demo_reads_the_reference_sample_clouds():
+    """The drop-in's own C++ PLY reader and host grid setup on the
+    reference's sample clouds (data/sample/3dmatch-demo, read in place where
+    the reference tree is mounted): vertex count, first and last point and
+    grid geometry equal the golden values derived by the oracle
+    (core/demo.cu:69-124)."""
+    import json
+    from conftest import golden, reference_path
+    _need_demo()
+    want = json.load(open(golden("sample_clouds.json")))
+    for name, g in want.items():
+        path = reference_path("data/sample/3dmatch-demo", name)
+        if not os.path.exists(path):
+            pytest.skip("reference sample clouds not mounted")
+        r = subprocess.run([DEMO, path, "/nonexistent/out", "--info"], capture_output=True)
+        assert r.returncode == 0, r.stderr.decode()
+        out = r.stdout.decode().split("\n")
+        assert "Loaded point cloud with %d points!" % g["n"] in out
+        tok = next(l for l in out if l.startswith("points ")).split()
+        assert int(tok[1]) == g["n"]
+        assert np.array_equal(np.float32(tok[3:6]), np.float32(g["first"]))
+        assert np.array_equal(np.float32(tok[7:10]), np.float32(g["last"]))
+        tok = next(l for l in out if l.startswith("grid ")).split()
+        assert [int(t) for t in tok[1:4]] == g["dim"]
+        assert np.array_equal(np.float32(tok[5:8]), np.float32(g["origin"]))
+
+
 @pytest.mark.gpu
 def test_demo_files_equal_library(tdm, scene, cuda, tmp_path):
     import torch

@@ -1,7 +1,10 @@
 """GPU parity of the descriptor net against the oracle.
 
 Tolerances: FP32 form <= 1e-4 relative L2 against the FP32 oracle forward;
-BF16 tensor-core form <= 1e-2 relative L2 against the FP64 oracle forward.
+BF16 tensor-core form <= 1e-2 relative L2 against the FP64 oracle forward and
+<= 1e-3 against the float64 restatement of its BF16 rounding; FP8 form <= 5e-3
+against the float64 restatement of its E4M3 rounding (its distance from the
+exact net, ~1e-1, is outside the 1e-2 descriptor tolerance).
 """
 import numpy as np
 import pytest
@@ -9,6 +12,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 RESPONSES = ["conv1", "conv2", "pool1", "conv3", "conv4", "conv5", "conv6", "conv7", "conv8", "feat"]
+FP8_LAYERS = (2, 3, 4, 5, 6, 7)  # conv3..conv8 take E4M3 operands in the FP8 form
+# The tensor-core kernels against the float64 restatement of their own operand
+# and storage rounding: only the FP32 accumulation order differs.
+BF16_KERNEL_TOL = 1e-3
+FP8_KERNEL_TOL = 5e-3
 
 
 def rel_l2(a, b):
@@ -146,19 +154,87 @@ def test_fp8_scales(fp8_net, oracle_resp):
         assert abs(sc[l] * 448 / oracle_resp[name].max() - 1) < 0.05, name
 
 
+@pytest.fixture(scope="module")
+def fp8_emulated(oracle, fp8_net, patches, weights):
+    """The FP8 form's arithmetic restated in float64: E4M3 operands for
+    conv3..conv8 with the net's own calibrated scales, BF16 elsewhere."""
+    return oracle.net_forward_quantized(patches.cpu().numpy()[:4], weights, FP8_LAYERS, fp8_net.act_scales(),
+                                        want=FP8_RESPONSES)
+
+
 @pytest.mark.parametrize("name", FP8_RESPONSES)
-def test_fp8_responses(fp8_net, patches, oracle_resp, name):
+def test_fp8_responses(fp8_net, patches, fp8_emulated, name):
+    """Each FP8-form response equals the float64 restatement of the same
+    E4M3/BF16 rounding (the kernels add in FP32, so a rare rounding step
+    lands differently)."""
     got = fp8_net.response(name, patches[:4]).cpu().numpy()
-    err = rel_l2(got, oracle_resp[name])
-    assert err <= 0.1, (name, err)  # E4M3 keeps 3 mantissa bits
+    err = rel_l2(got, fp8_emulated[1][name])
+    assert err <= FP8_KERNEL_TOL, (name, err)
 
 
-def test_fp8_descriptors(tdm, oracle, fp8_net, weights, patches):
-    got = fp8_net.forward(patches).cpu().numpy()
-    want64 = oracle.net_forward(patches.cpu().numpy(), weights, f64=True)
+def test_fp8_descriptors(tdm, oracle, fp8_net, weights, patches, fp8_emulated):
+    """FP8 descriptors equal the E4M3 restatement; their distance from the
+    exact FP64 net is what E4M3 rounding gives (about 3.5e-2 per E4M3 layer,
+    8e-2 to 1e-1 for conv3..conv8), outside the 1e-2 descriptor tolerance
+    that the BF16 form meets."""
+    got = fp8_net.forward(patches[:4].contiguous()).cpu().numpy()
+    assert rel_l2(got, fp8_emulated[0]) <= FP8_KERNEL_TOL
+    want64 = oracle.net_forward(patches.cpu().numpy()[:4], weights, f64=True)
+    err, emu = rel_l2(got, want64), rel_l2(fp8_emulated[0], want64)
+    print("fp8 descriptor rel-L2 vs FP64: %.4g (restatement %.4g)" % (err, emu))
+    assert abs(err - emu) <= 0.1 * emu
+    tdm.device_status()
+
+
+def test_bf16_equals_its_rounding_restatement(tdm, oracle, weights, patches):
+    """The BF16 kernels compute the BF16-rounded net: against the float64
+    restatement of the same rounding they agree far inside the BF16 error."""
+    net = tdm.Net(weights, precision="bf16")
+    got = net.forward(patches).cpu().numpy()
+    want = oracle.net_forward_quantized(patches.cpu().numpy(), weights)
+    assert rel_l2(got, want) <= BF16_KERNEL_TOL
+    tdm.device_status()
+
+
+@pytest.fixture(scope="module")
+def chunk_patches(tdm, scene, cuda):
+    """2,048 pipeline patches: one full internal chunk of the net, the launch
+    size the pair bench times (persistent tile loops with many tiles per CTA,
+    conv8's four-way split K)."""
+    import torch
+    pts = scene.fragment(20260004)
+    g = tdm.grid_from_points_host(pts)
+    pd = torch.from_numpy(pts).to(cuda)
+    tdf = tdm.tdf(pd, g)
+    idx = tdm.keypoint_indices(11, pts.shape[0], 2048, device=cuda)
+    _, kg = tdm.keypoints(pd, idx, g)
+    return tdm.gather(tdf, g, kg)
+
+
+# 16 patches spread over the chunk: both ends, tile and sub-tile edges, the rest seeded
+SAMPLED = sorted(set([0, 1, 127, 128, 1023, 1024, 2046, 2047] +
+                     np.random.default_rng(5).choice(2048, 8, replace=False).tolist()))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "fp8"])
+def test_descriptors_at_the_timed_launch_size(tdm, oracle, weights, chunk_patches, precision):
+    net = tdm.Net(weights, precision=precision)
+    if precision == "fp8":
+        net.calibrate(chunk_patches[:256].contiguous())
+    got = net.forward(chunk_patches).cpu().numpy()[SAMPLED]
+    p = chunk_patches.cpu().numpy()[SAMPLED]
+    want64 = oracle.net_forward(p, weights, f64=True)
     err = rel_l2(got, want64)
-    print("fp8 descriptor rel-L2 vs FP64:", err)
-    assert err <= 0.1
+    print(precision, "2048-patch launch, 16 sampled descriptors, rel-L2 vs FP64: %.4g" % err)
+    if precision == "fp32":
+        assert err <= 1e-4
+    elif precision == "bf16":
+        assert err <= 1e-2
+        assert rel_l2(got, oracle.net_forward_quantized(p, weights)) <= BF16_KERNEL_TOL
+    else:
+        emu = oracle.net_forward_quantized(p, weights, FP8_LAYERS, net.act_scales())
+        assert rel_l2(got, emu) <= FP8_KERNEL_TOL
+    net.close()
     tdm.device_status()
 
 
@@ -201,4 +277,24 @@ def test_fused_x_pool_same_bits(tdm, weights, patches, precision):
     p1 = net.response("pool1", b).cpu().numpy()   # [b, 13, 13, 13, 64], fused x-pair max
     want = c2.reshape(6, 13, 2, 13, 2, 13, 2, 64).max(axis=(2, 4, 6))
     assert np.array_equal(p1, want)
+    tdm.device_status()
+
+
+def test_half_typed_marvin_file(tdm, oracle, weights, patches, tmp_path):
+    """A .marvin file whose records are half (type id 0), as Marvin writes
+    weights when StorageT is half (core/marvin.hpp:2634-2705, 467-550 for
+    the conversion): tdm_net_create decodes them to the half-rounded floats,
+    and the FP32 net equals the oracle forward on those rounded weights."""
+    path = str(tmp_path / "half.marvin")
+    oracle.write_marvin(path, weights, dtype=np.float16)
+    assert oracle.read_marvin(path)["conv1.weight"].dtype == np.float16
+    rounded = {k: v.astype(np.float16).astype(np.float32) for k, v in weights.items()}
+    net = tdm.Net(precision="fp32", marvin_path=path)
+    got = net.forward(patches).cpu().numpy()
+    p = patches.cpu().numpy()
+    want = oracle.net_forward(p, rounded)
+    assert rel_l2(got, want) <= 1e-4
+    # and not the unrounded weights' output (half rounding moves descriptors ~1e-3)
+    assert rel_l2(got, oracle.net_forward(p, weights)) > 10 * rel_l2(got, want)
+    net.close()
     tdm.device_status()

@@ -81,3 +81,44 @@ def test_register_pair_host_equals_device(tdm, cuda, pair, weights):
     r_host = pipe.register(a, b, seed=7, k=500)
     assert r_dev.n_matches == r_host.n_matches and r_dev.best_trial == r_host.best_trial
     assert np.array_equal(np.array(r_dev.rt), np.array(r_host.rt))
+
+
+def test_bf16_nearest_neighbours_agree_where_fp32_separates_them(tdm, oracle, cuda, pair, weights):
+    """Real pipeline descriptors of C1 shape (1,000 keypoints on each fragment
+    of a synthetic pair, 30^3 patches, random He-normal weights): wherever the
+    FP32 form's nearest neighbour is more than 5 % closer than its second
+    (second / first distance > 1.05, exact FP64 distances), the BF16 form --
+    BF16 descriptors and the BF16 distance GEMM -- returns the same nearest
+    neighbour (core/demo.m:51-57 nn), in both directions.  Random weights
+    leave most descriptors nearly equidistant; the rows below the margin are
+    reported, not asserted."""
+    import torch
+    a, b, _ = pair
+    k = 1000
+    nets = {p: tdm.Net(weights, precision=p) for p in ("fp32", "bf16")}
+    desc = {}
+    for p, net in nets.items():
+        pipe = tdm.Pipeline(net, max_keypoints=k)
+        da = pipe.describe(torch.from_numpy(a).to(cuda), seed=3, k=k)[1]
+        db = pipe.describe(torch.from_numpy(b).to(cuda), seed=4, k=k)[1]
+        desc[p] = (da, db)
+        pipe.close()
+    _, _, ab32, ba32 = tdm.match_mnn(*desc["fp32"], precision="fp32")
+    _, _, ab16, ba16 = tdm.match_mnn(*desc["bf16"], precision="bf16")
+    f32a, f32b = (x.cpu().numpy() for x in desc["fp32"])
+    _, ref_ab, ref_ba = oracle.mutual_nn(f32a, f32b)
+    d32a, d32b = f32a.astype(np.float64), f32b.astype(np.float64)
+    report = []
+    for q, r, nn32, nn16, ref in ((d32a, d32b, ab32, ab16, ref_ab), (d32b, d32a, ba32, ba16, ref_ba)):
+        d2 = (q * q).sum(1)[:, None] + (r * r).sum(1)[None, :] - 2.0 * q @ r.T
+        d = np.sqrt(np.maximum(d2, 0.0))
+        two = np.sort(d, axis=1)[:, :2]
+        margin = two[:, 1] / np.maximum(two[:, 0], 1e-30)
+        sep = margin > 1.05
+        nn32, nn16 = nn32.cpu().numpy(), nn16.cpu().numpy()
+        assert np.array_equal(nn32, ref)  # the FP32 form is the exact NN
+        assert sep.sum() >= 20
+        assert np.array_equal(nn16[sep], nn32[sep]), int((nn16[sep] != nn32[sep]).sum())
+        report.append((int(sep.sum()), float(np.mean(nn16 == nn32))))
+    print("rows with FP32 margin > 5 %% / BF16 agreement over all rows: %s" % report)
+    tdm.device_status()
