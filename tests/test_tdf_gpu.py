@@ -143,3 +143,36 @@ def test_nonfinite_points_are_skipped_by_both_grid_forms(tdm, oracle, cuda, smal
     with pytest.raises(RuntimeError):
         tdm.grid_from_points(torch.from_numpy(bad).to(cuda))
     tdm.device_status()
+
+
+def test_refcompat_decode_equals_the_reference_kernel(tdm, oracle, cuda, frag):
+    """The reference's own ComputeTDF (core/demo.cu:22-57, extracted and built
+    by oracle/ref_tdf.py with the reference's compile flags) on a 29M-voxel
+    grid: its float32 index decode lands about a fifth of the voxels past
+    2^24 on the wrong centre.  TDM_TDF_REFCOMPAT_FMA gives its bits on every
+    voxel; the exact decode differs where the quirk bites."""
+    import torch
+    from oracle import ref_tdf
+    L = ref_tdf.lib()
+    if L is None:
+        pytest.skip("reference TDF kernel not extracted (reference tree absent when the tests were prepared)")
+    g = tdm.grid_from_points_host(frag)
+    dim, origin, occ = _occ(oracle, frag)
+    V = int(np.prod(dim.astype(np.int64)))
+    assert V > (1 << 24)
+    occ_f = torch.zeros(V + 1, dtype=torch.float32, device=cuda)  # V + 1: the kernel touches index V
+    occ_f[:V] = torch.from_numpy(occ.astype(np.float32)).to(cuda)
+    ref = torch.zeros(V + 1, dtype=torch.float32, device=cuda)
+    torch.cuda.synchronize()
+    rc = L.ref_compute_tdf(occ_f.data_ptr(), ref.data_ptr(), int(dim[0]), int(dim[1]), int(dim[2]),
+                           float(g.origin[0]), float(g.origin[1]), float(g.origin[2]), float(g.voxel_size),
+                           float(g.trunc_margin))
+    assert rc == 0
+    ref = ref[:V].cpu().numpy()
+    pd = torch.from_numpy(frag).to(cuda)
+    fma = tdm.tdf(pd, g, mode=tdm.TDF_REFCOMPAT_FMA).cpu().numpy()
+    assert np.array_equal(fma, ref), int((fma != ref).sum())
+    exact = tdm.tdf(pd, g).cpu().numpy()
+    assert int((exact != ref).sum()) > 0
+    print("voxels where the reference's decode changes the TDF: %d of %d" % (int((exact != ref).sum()), V))
+    tdm.device_status()
