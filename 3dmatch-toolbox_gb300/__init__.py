@@ -40,6 +40,9 @@ EXPORTS = [
     "tdm_pipeline_create", "tdm_pipeline_destroy", "tdm_describe_fragment", "tdm_register_pair",
     "tdm_register_pair_host", "tdm_net_clone", "tdm_net_workspace_bytes",
     "tdm_server_create", "tdm_server_slots", "tdm_server_submit", "tdm_server_wait", "tdm_server_destroy",
+    "tdm_server_submit_pair", "tdm_server_cancel", "tdm_server_get_stats",
+    "tdm_store_create", "tdm_store_destroy", "tdm_store_describe", "tdm_store_put", "tdm_store_get",
+    "tdm_store_remove", "tdm_store_get_stats", "tdm_register_stored",
     "tdm_net_autotune", "tdm_net_tiles", "tdm_net_set_tile", "tdm_net_tile_forms", "tdm_net_set_tile_form",
     "tdm_batch_create", "tdm_batch_destroy", "tdm_batch_device_bytes", "tdm_describe_batch", "tdm_batch_stats",
     "tdm_overlap_workspace_bytes", "tdm_overlap", "tdm_tdf_exact", "tdm_icp_workspace_bytes", "tdm_icp",
@@ -93,7 +96,32 @@ class IcpResult(ctypes.Structure):
 
 
 class ServerConfig(ctypes.Structure):
-    _fields_ = [("pipeline", PipelineConfig), ("slots", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64)]
+    _fields_ = [("pipeline", PipelineConfig), ("slots", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64),
+                ("store_bytes", ctypes.c_int64)]
+
+
+class Fragment(ctypes.Structure):
+    _fields_ = [("key", ctypes.c_uint64), ("pts", ctypes.c_void_p), ("n", ctypes.c_int32), ("seed", ctypes.c_uint64),
+                ("k", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("requests_done", ctypes.c_int64), ("requests_cancelled", ctypes.c_int64), ("waves", ctypes.c_int64),
+                ("fragments_described", ctypes.c_int64), ("store_hits", ctypes.c_int64),
+                ("store_entries", ctypes.c_int64), ("max_wave_requests", ctypes.c_int64),
+                ("device_bytes", ctypes.c_int64), ("describe_ms", ctypes.c_double), ("match_ms", ctypes.c_double),
+                ("overlap_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class StoreStats(ctypes.Structure):
+    _fields_ = [("entries", ctypes.c_int64), ("bytes_used", ctypes.c_int64), ("capacity", ctypes.c_int64),
+                ("hits", ctypes.c_int64), ("misses", ctypes.c_int64), ("evictions", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 
 class PairResult(ctypes.Structure):
@@ -162,7 +190,20 @@ def lib():
         "tdm_server_create": (i32, [ctypes.POINTER(ServerConfig), P, ctypes.POINTER(P)]),
         "tdm_server_slots": (i32, [P]),
         "tdm_server_submit": (i32, [P, P, i32, P, i32, u64, i32, ctypes.POINTER(ctypes.c_int64)]),
-        "tdm_server_wait": (i32, [P, ctypes.c_int64, ctypes.POINTER(PairResult), ctypes.POINTER(ctypes.c_double)]),
+        "tdm_server_wait": (i32, [P, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(PairResult),
+                                  ctypes.POINTER(ctypes.c_double)]),
+        "tdm_server_submit_pair": (i32, [P, ctypes.POINTER(Fragment), ctypes.POINTER(Fragment),
+                                         ctypes.POINTER(ctypes.c_int64)]),
+        "tdm_server_cancel": (i32, [P, ctypes.c_int64]),
+        "tdm_server_get_stats": (i32, [P, ctypes.POINTER(ServerStats)]),
+        "tdm_store_create": (i32, [i64, ctypes.POINTER(P)]),
+        "tdm_store_destroy": (i32, [P]),
+        "tdm_store_describe": (i32, [P, P, u64, P, i32, u64, i32, ctypes.POINTER(i32), P]),
+        "tdm_store_put": (i32, [P, u64, u64, P, P, i32, G, P]),
+        "tdm_store_get": (i32, [P, u64, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(i32), G]),
+        "tdm_store_remove": (i32, [P, u64]),
+        "tdm_store_get_stats": (i32, [P, ctypes.POINTER(StoreStats)]),
+        "tdm_register_stored": (i32, [P, P, u64, u64, ctypes.POINTER(PairResult), P]),
         "tdm_server_destroy": (i32, [P]),
         "tdm_net_autotune": (i32, [P, P, i32, i32, P]),
         "tdm_net_tiles": (i32, [P, P, P]),
@@ -578,6 +619,74 @@ class Pipeline:
             pass
 
 
+class Store:
+    """Device-resident fragment store (tdm_store): describe once, register many."""
+
+    def __init__(self, budget_bytes: int):
+        h = ctypes.c_void_p()
+        check(lib().tdm_store_create(budget_bytes, ctypes.byref(h)))
+        self.handle = h
+
+    def describe(self, pipe: "Pipeline", key: int, pts_dev, seed: int, k: int, stream=None) -> bool:
+        """Describes the fragment under `key` unless stored; returns whether it was a hit."""
+        hit = ctypes.c_int32()
+        check(lib().tdm_store_describe(self.handle, pipe.handle, key, _ptr(pts_dev), pts_dev.shape[0], seed, k,
+                                       ctypes.byref(hit), _stream(stream)))
+        return bool(hit.value)
+
+    def put(self, key: int, seed: int, keypts_dev, desc_dev, grid: Grid = None, stream=None) -> None:
+        check(lib().tdm_store_put(self.handle, key, seed, _ptr(keypts_dev), _ptr(desc_dev), keypts_dev.shape[0],
+                                  ctypes.byref(grid) if grid is not None else None, _stream(stream)))
+
+    def get(self, key: int, device="cuda"):
+        """Copies of the stored keypoints and descriptors (torch tensors) and the grid."""
+        import torch
+        kp, desc, k, g = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_int32(), Grid()
+        check(lib().tdm_store_get(self.handle, key, ctypes.byref(kp), ctypes.byref(desc), ctypes.byref(k),
+                                  ctypes.byref(g)))
+        n = k.value
+        torch.cuda.synchronize()
+        return (_device_view(kp.value, (n, 3), device).clone(), _device_view(desc.value, (n, 512), device).clone(), g)
+
+    def remove(self, key: int) -> None:
+        check(lib().tdm_store_remove(self.handle, key))
+
+    def stats(self) -> dict:
+        st = StoreStats()
+        check(lib().tdm_store_get_stats(self.handle, ctypes.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if self.handle:
+            lib().tdm_store_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _CudaArray:
+    """A float32 device buffer described by __cuda_array_interface__."""
+
+    def __init__(self, ptr: int, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f4", "data": (ptr, False),
+                                         "version": 2, "strides": None}
+
+
+def _device_view(ptr: int, shape, device="cuda"):
+    import torch
+    return torch.as_tensor(_CudaArray(ptr, shape), device=device)
+
+
+def register_stored(pipe: "Pipeline", store: Store, key_a: int, key_b: int, stream=None) -> PairResult:
+    r = PairResult()
+    check(lib().tdm_register_stored(pipe.handle, store.handle, key_a, key_b, ctypes.byref(r), _stream(stream)))
+    return r
+
+
 class Batch:
     """Many fragments of uneven size through one persistent launch per stage
     (tdm_describe_batch); with use_graph the sequence is replayed as a CUDA graph."""
@@ -636,11 +745,11 @@ class Batch:
 
 
 class Server:
-    """Serving loop: requests queue up and run on min(slots, budget / slot
-    footprint) concurrent slots (own stream, buffers and net clone each)."""
+    """tdm_server: continuous batching of pair registrations over the batched
+    description kernels and a device-resident fragment store."""
 
-    def __init__(self, net: Net, slots=4, hbm_budget_bytes=120 << 30, **pipeline_kw):
-        cfg = ServerConfig(pipeline_config(**pipeline_kw), slots, hbm_budget_bytes)
+    def __init__(self, net: Net, slots=4, hbm_budget_bytes=120 << 30, store_bytes=0, **pipeline_kw):
+        cfg = ServerConfig(pipeline_config(**pipeline_kw), slots, hbm_budget_bytes, store_bytes)
         h = ctypes.c_void_p()
         check(lib().tdm_server_create(ctypes.byref(cfg), net.handle, ctypes.byref(h)))
         self.handle = h
@@ -656,11 +765,34 @@ class Server:
         check(lib().tdm_server_submit(self.handle, _ptr(a), a.shape[0], _ptr(b), b.shape[0], seed, k, ctypes.byref(t)))
         return t.value
 
-    def wait(self, ticket: int):
+    def submit_pair(self, a: dict, b: dict) -> int:
+        """a, b: {"key": int (0 = anonymous), "pts": array or None, "seed": int, "k": int}."""
+        frags, keep = [], []
+        for f in (a, b):
+            pts = f.get("pts")
+            if pts is not None:
+                pts = np.ascontiguousarray(pts, np.float32)
+                keep.append(pts)
+            frags.append(Fragment(f.get("key", 0), _ptr(pts) if pts is not None else None,
+                                  pts.shape[0] if pts is not None else 0, f["seed"], f["k"]))
+        t = ctypes.c_int64()
+        check(lib().tdm_server_submit_pair(self.handle, ctypes.byref(frags[0]), ctypes.byref(frags[1]),
+                                           ctypes.byref(t)))
+        return t.value
+
+    def cancel(self, ticket: int) -> None:
+        check(lib().tdm_server_cancel(self.handle, ticket))
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
         r = PairResult()
         lat = ctypes.c_double()
-        check(lib().tdm_server_wait(self.handle, ticket, ctypes.byref(r), ctypes.byref(lat)))
+        check(lib().tdm_server_wait(self.handle, ticket, timeout_ms, ctypes.byref(r), ctypes.byref(lat)))
         return r, lat.value
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(lib().tdm_server_get_stats(self.handle, ctypes.byref(st)))
+        return st.as_dict()
 
     def close(self):
         if self.handle:

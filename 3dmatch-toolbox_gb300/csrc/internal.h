@@ -112,4 +112,33 @@ tdm_precision net_precision(const tdm_net* net);
 // changes: a CUDA graph holding a forward of the net is stale after that.
 uint64_t net_generation(const tdm_net* net);
 
+// ---- store.cpp: device-resident fragment store ----
+struct StoreView {
+  const float* keypts;  // k x 3
+  const float* desc;    // k x 512
+  int32_t k;
+  tdm_grid grid;
+};
+// Reserves (or replaces) entry `key` for k keypoints and returns where to
+// write it; the entry is pinned and invisible to readers until committed.
+tdm_status store_reserve(tdm_store* st, uint64_t key, uint64_t seed, int32_t k, const tdm_grid* grid, float** keypts,
+                         float** desc);
+// Ends a write (records the entry's ready event on s); ok = false drops it.
+tdm_status store_commit(tdm_store* st, uint64_t key, const tdm_grid* grid, bool ok, cudaStream_t s);
+// Pins an entry for reading on stream s (s waits for the entry's writer).
+tdm_status store_acquire(tdm_store* st, uint64_t key, StoreView* v, cudaStream_t s);
+// Pins an entry against eviction (no stream ordering); false if absent.
+bool store_pin(tdm_store* st, uint64_t key);
+void store_release(tdm_store* st, uint64_t key);
+// Entry present with this keypoint stream and count; `count` updates the
+// hit / miss counters and the entry's recency.
+bool store_has(tdm_store* st, uint64_t key, uint64_t seed, int32_t k, bool count);
+size_t store_entry_bytes(int32_t k);
+
+// ---- pipeline.cu ----
+// A pipeline holding only the matching and RANSAC buffers (for pairs of
+// already described fragments of up to cfg->max_keypoints keypoints).
+tdm_status pipeline_create_match_only(const tdm_pipeline_config* cfg, tdm_pipeline** out);
+size_t pipeline_match_bytes(const tdm_pipeline_config* cfg);
+
 }  // namespace tdm

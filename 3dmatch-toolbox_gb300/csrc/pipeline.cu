@@ -50,16 +50,73 @@ struct tdm_pipeline {
 
 using namespace tdm;
 
-extern "C" tdm_status tdm_pipeline_create(const tdm_pipeline_config* cfg, tdm_net* net, tdm_pipeline** out) {
-  TDM_REQUIRE(cfg && net && out, "tdm_pipeline_create: null pointer");
+namespace {
+
+// Matching and RANSAC buffers for fragments of up to K keypoints.
+tdm_status alloc_match(tdm_pipeline* p, size_t K) {
+  tdm_status st = TDM_OK;
+  p->mnn_bytes = tdm_mnn_workspace_bytes((int)K, (int)K, 512);
+  if (!st) st = p->alloc(&p->mnn_ws, p->mnn_bytes);
+  if (!st) st = p->alloc(&p->nn_ab, K * 4);
+  if (!st) st = p->alloc(&p->nn_ba, K * 4);
+  if (!st) st = p->alloc(&p->pairs, K * 8);
+  if (!st) st = p->alloc(&p->npairs, 4);
+  if (!st) st = p->alloc(&p->x, K * 12);
+  if (!st) st = p->alloc(&p->y, K * 12);
+  p->rws_bytes = tdm_ransac_workspace_bytes((int)K, p->cfg.ransac.iterations);
+  if (!st) st = p->alloc(&p->rws, p->rws_bytes);
+  if (!st) st = p->alloc(&p->rt, 12 * 8);
+  if (!st) st = p->alloc(&p->inliers, K * 4);
+  if (!st) st = p->alloc(&p->info, 16);
+  if (!st) {
+    cudaError_t e = cudaMallocHost(&p->host_stage, 256);
+    if (e != cudaSuccess) st = cuda_status(e, "pinned staging");
+  }
+  return st;
+}
+
+tdm_status check_config(const tdm_pipeline_config* cfg) {
   TDM_REQUIRE(cfg->voxel_size > 0 && cfg->trunc_voxels > 0 && cfg->pad >= 0, "tdm_pipeline_create: bad grid");
   TDM_REQUIRE(cfg->max_points > 0 && cfg->max_keypoints > 0 && cfg->max_voxels > 0, "tdm_pipeline_create: bad sizes");
   TDM_REQUIRE(cfg->ransac.iterations >= 0 && cfg->ransac.threshold > 0, "tdm_pipeline_create: bad RANSAC params");
+  return TDM_OK;
+}
+
+}  // namespace
+
+namespace tdm {
+
+size_t pipeline_match_bytes(const tdm_pipeline_config* cfg) {
+  const size_t K = (size_t)cfg->max_keypoints;
+  return tdm_mnn_workspace_bytes((int)K, (int)K, 512) + K * 52 + 256 +
+         tdm_ransac_workspace_bytes((int)K, cfg->ransac.iterations);
+}
+
+tdm_status pipeline_create_match_only(const tdm_pipeline_config* cfg, tdm_pipeline** out) {
+  TDM_REQUIRE(cfg && out, "pipeline: null pointer");
+  tdm_status st = check_config(cfg);
+  if (st) return st;
+  tdm_pipeline* p = new tdm_pipeline();
+  p->cfg = *cfg;
+  st = alloc_match(p, (size_t)cfg->max_keypoints);
+  if (st) {
+    delete p;
+    return st;
+  }
+  *out = p;
+  return TDM_OK;
+}
+
+}  // namespace tdm
+
+extern "C" tdm_status tdm_pipeline_create(const tdm_pipeline_config* cfg, tdm_net* net, tdm_pipeline** out) {
+  TDM_REQUIRE(cfg && net && out, "tdm_pipeline_create: null pointer");
+  tdm_status st = check_config(cfg);
+  if (st) return st;
   tdm_pipeline* p = new tdm_pipeline();
   p->cfg = *cfg;
   p->net = net;
   const size_t K = (size_t)cfg->max_keypoints, N = (size_t)cfg->max_points, V = (size_t)cfg->max_voxels;
-  tdm_status st = TDM_OK;
   for (int f = 0; f < 2 && st == TDM_OK; ++f) {
     st = p->alloc(&p->pts[f], N * 12);
     if (!st) st = p->alloc(&p->idx[f], K * 4);
@@ -71,23 +128,7 @@ extern "C" tdm_status tdm_pipeline_create(const tdm_pipeline_config* cfg, tdm_ne
   if (!st) st = p->alloc(&p->grid_ws, tdm_grid_workspace_bytes());
   if (!st) st = p->alloc(&p->patches, 2 * K * 27000 * 4);
   if (!st) st = p->alloc(&p->desc, 2 * K * 512 * 4);
-  p->mnn_bytes = tdm_mnn_workspace_bytes((int)K, (int)K, 512);
-  if (!st) st = p->alloc(&p->mnn_ws, p->mnn_bytes);
-  if (!st) st = p->alloc(&p->nn_ab, K * 4);
-  if (!st) st = p->alloc(&p->nn_ba, K * 4);
-  if (!st) st = p->alloc(&p->pairs, K * 8);
-  if (!st) st = p->alloc(&p->npairs, 4);
-  if (!st) st = p->alloc(&p->x, K * 12);
-  if (!st) st = p->alloc(&p->y, K * 12);
-  p->rws_bytes = tdm_ransac_workspace_bytes((int)K, cfg->ransac.iterations);
-  if (!st) st = p->alloc(&p->rws, p->rws_bytes);
-  if (!st) st = p->alloc(&p->rt, 12 * 8);
-  if (!st) st = p->alloc(&p->inliers, K * 4);
-  if (!st) st = p->alloc(&p->info, 16);
-  if (!st) {
-    cudaError_t e = cudaMallocHost(&p->host_stage, 256);
-    if (e != cudaSuccess) st = cuda_status(e, "pinned staging");
-  }
+  if (!st) st = alloc_match(p, K);
   if (st) {
     delete p;
     return st;
@@ -117,15 +158,17 @@ tdm_status fragment_front(tdm_pipeline* p, int f, const float* pts, int32_t n, c
   return tdm_gather(p->tdf[f], &g, p->kpg[f], k, patches, s);
 }
 
-tdm_status pair_back(tdm_pipeline* p, int32_t k, const tdm_grid g[2], tdm_pair_result* r, cudaStream_t s) {
-  tdm_status st = tdm_net_forward(p->net, p->patches, 2 * k, p->desc, s);
+// core/demo.m:49-64 on two described fragments: mutual NN of the
+// descriptors, the matched keypoints, RANSAC + refit; result copied to host.
+tdm_status match_back(tdm_pipeline* p, const float* desc_a, const float* kp_a, int32_t ka, const float* desc_b,
+                      const float* kp_b, int32_t kb, const tdm_grid g[2], tdm_pair_result* r, cudaStream_t s) {
+  const int32_t m_max = ka < kb ? ka : kb;
+  tdm_status st = tdm_match_mnn(desc_a, ka, desc_b, kb, 512, p->cfg.match_precision, p->nn_ab, p->nn_ba, p->pairs,
+                                p->npairs, p->mnn_ws, p->mnn_bytes, s);
   if (st) return st;
-  st = tdm_match_mnn(p->desc, k, p->desc + (size_t)k * 512, k, 512, p->cfg.match_precision, p->nn_ab, p->nn_ba,
-                     p->pairs, p->npairs, p->mnn_ws, p->mnn_bytes, s);
+  st = tdm_pairs_to_points(kp_a, kp_b, p->pairs, p->npairs, m_max, p->x, p->y, s);
   if (st) return st;
-  st = tdm_pairs_to_points(p->kp[0], p->kp[1], p->pairs, p->npairs, k, p->x, p->y, s);
-  if (st) return st;
-  st = tdm_ransac(p->x, p->y, p->npairs, k, &p->cfg.ransac, p->rt, p->inliers, p->info, p->rws, p->rws_bytes, s);
+  st = tdm_ransac(p->x, p->y, p->npairs, m_max, &p->cfg.ransac, p->rt, p->inliers, p->info, p->rws, p->rws_bytes, s);
   if (st) return st;
   double* h_rt = static_cast<double*>(p->host_stage);
   int32_t* h_info = reinterpret_cast<int32_t*>(h_rt + 12);
@@ -139,17 +182,24 @@ tdm_status pair_back(tdm_pipeline* p, int32_t k, const tdm_grid g[2], tdm_pair_r
   r->n_inliers = h_info[0];
   r->best_trial = h_info[1];
   r->n_matches = h_info[4];
-  r->keypoints[0] = r->keypoints[1] = k;
+  r->keypoints[0] = ka;
+  r->keypoints[1] = kb;
   for (int f = 0; f < 2; ++f)
     for (int a = 0; a < 3; ++a) r->grid_dim[f][a] = g[f].dim[a];
   return TDM_OK;
+}
+
+tdm_status pair_back(tdm_pipeline* p, int32_t k, const tdm_grid g[2], tdm_pair_result* r, cudaStream_t s) {
+  tdm_status st = tdm_net_forward(p->net, p->patches, 2 * k, p->desc, s);
+  if (st) return st;
+  return match_back(p, p->desc, p->kp[0], k, p->desc + (size_t)k * 512, p->kp[1], k, g, r, s);
 }
 
 }  // namespace
 
 extern "C" tdm_status tdm_describe_fragment(tdm_pipeline* p, const float* pts, int32_t n, uint64_t seed, int32_t k,
                                             float* keypts, float* desc, tdm_grid* grid_out, tdm_stream s) {
-  TDM_REQUIRE(p && pts && keypts && desc && n > 0 && k > 0, "tdm_describe_fragment: bad arguments");
+  TDM_REQUIRE(p && pts && keypts && desc && n > 0 && k > 0 && p->net, "tdm_describe_fragment: bad arguments");
   TDM_REQUIRE(n <= p->cfg.max_points && k <= p->cfg.max_keypoints, "tdm_describe_fragment: exceeds pipeline limits");
   tdm_grid g;
   const float trunc = p->cfg.voxel_size * p->cfg.trunc_voxels;
@@ -165,7 +215,7 @@ extern "C" tdm_status tdm_describe_fragment(tdm_pipeline* p, const float* pts, i
 
 extern "C" tdm_status tdm_register_pair(tdm_pipeline* p, const float* a, int32_t na, const float* b, int32_t nb,
                                         uint64_t seed, int32_t k, tdm_pair_result* r, tdm_stream s) {
-  TDM_REQUIRE(p && a && b && r && na > 0 && nb > 0 && k > 0, "tdm_register_pair: bad arguments");
+  TDM_REQUIRE(p && a && b && r && na > 0 && nb > 0 && k > 0 && p->net, "tdm_register_pair: bad arguments");
   TDM_REQUIRE(na <= p->cfg.max_points && nb <= p->cfg.max_points && k <= p->cfg.max_keypoints,
               "tdm_register_pair: exceeds pipeline limits");
   const float trunc = p->cfg.voxel_size * p->cfg.trunc_voxels;
@@ -185,7 +235,7 @@ extern "C" tdm_status tdm_register_pair(tdm_pipeline* p, const float* a, int32_t
 
 extern "C" tdm_status tdm_register_pair_host(tdm_pipeline* p, const float* a, int32_t na, const float* b, int32_t nb,
                                              uint64_t seed, int32_t k, tdm_pair_result* r, tdm_stream s) {
-  TDM_REQUIRE(p && a && b && r && na > 0 && nb > 0 && k > 0, "tdm_register_pair_host: bad arguments");
+  TDM_REQUIRE(p && a && b && r && na > 0 && nb > 0 && k > 0 && p->net, "tdm_register_pair_host: bad arguments");
   TDM_REQUIRE(na <= p->cfg.max_points && nb <= p->cfg.max_points && k <= p->cfg.max_keypoints,
               "tdm_register_pair_host: exceeds pipeline limits");
   const float trunc = p->cfg.voxel_size * p->cfg.trunc_voxels;
@@ -204,4 +254,26 @@ extern "C" tdm_status tdm_register_pair_host(tdm_pipeline* p, const float* a, in
     if (st) return st;
   }
   return pair_back(p, k, g, r, s);
+}
+
+extern "C" tdm_status tdm_register_stored(tdm_pipeline* p, tdm_store* store, uint64_t key_a, uint64_t key_b,
+                                          tdm_pair_result* r, tdm_stream s) {
+  TDM_REQUIRE(p && store && r, "tdm_register_stored: null pointer");
+  StoreView va{}, vb{};
+  tdm_status st = store_acquire(store, key_a, &va, s);
+  if (st) return st;
+  st = store_acquire(store, key_b, &vb, s);
+  if (st) {
+    store_release(store, key_a);
+    return st;
+  }
+  if (va.k > p->cfg.max_keypoints || vb.k > p->cfg.max_keypoints)
+    st = fail(TDM_ERR_INVALID_ARG, "tdm_register_stored: fragment has more keypoints than the pipeline's max_keypoints");
+  const tdm_grid g[2] = {va.grid, vb.grid};
+  // match_back synchronizes the stream, so the entries are no longer read
+  // when they are released
+  if (!st) st = match_back(p, va.desc, va.keypts, va.k, vb.desc, vb.keypts, vb.k, g, r, s);
+  store_release(store, key_a);
+  store_release(store, key_b);
+  return st;
 }

