@@ -885,14 +885,6 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
 // ---------------------------------------------------------------------------
 constexpr int kDxfNt = 32;
 constexpr int kDxfN = 3 * kDxfNt;
-// N of the MMA and TMEM columns per sub-tile: the B operand's 96 weight rows
-// (layout stride kDxfN), read as TDM_DXF_NMMA rows; rows past 96 are the next
-// chunk's (or the slab's) bytes and land in accumulator columns never read.
-#ifndef TDM_DXF_NMMA
-#define TDM_DXF_NMMA 96
-#endif
-constexpr int kDxfNmma = TDM_DXF_NMMA;
-static_assert(kDxfNmma >= kDxfN && kDxfNmma % 16 == 0 && kDxfNmma <= 128, "dx-fused MMA N");
 constexpr int kDxfSub = 126;
 constexpr uint32_t kDxfBlock = 8u * kDxfN * 16u;       // one (dz, dy): 8 K chunks x 96 rows x 16 B
 constexpr uint32_t kDxfWBytes = 9u * kDxfBlock;         // one half's weights
@@ -914,7 +906,7 @@ template <int MSUB, bool FP8_OUT, bool XPOOL>
 __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams p) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr int MOUT = MSUB * kDxfSub;
-  constexpr uint32_t ACC_COLS = MSUB * kDxfNmma;
+  constexpr uint32_t ACC_COLS = MSUB * kDxfN;
   constexpr uint32_t TMEM_COLS = tmem_cols_for(2 * ACC_COLS);
   static_assert(2 * ACC_COLS <= 512, "two accumulator buffers must fit in TMEM");
   const int R = p.R;
@@ -999,7 +991,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
-      constexpr uint32_t idesc = ptx::make_idesc(kDxfNmma, 128, 1, 1);
+      constexpr uint32_t idesc = ptx::make_idesc(kDxfN, 128, 1, 1);
       const uint32_t lboA = (uint32_t)R * 16u;
       const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), wDesc0 = ptx::smem_desc(sW_u, kDxfN * 16, 128);
 #ifdef TDM_WAIT_STATS
@@ -1038,7 +1030,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
 #ifdef TDM_WAIT_STATS
                 const long long c_issue = clock64();
 #endif
-                ptx::mma_f16(dbase + i * kDxfNmma, adesc, bdesc, idesc, accumulate);
+                ptx::mma_f16(dbase + i * kDxfN, adesc, bdesc, idesc, accumulate);
 #ifdef TDM_WAIT_STATS
                 issue_cycles += clock64() - c_issue;
 #endif
@@ -1089,7 +1081,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
         ptx::tc_fence_after();
 #pragma unroll
         for (int i = 0; i < MSUB; ++i) {
-          const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + i * kDxfNmma;
+          const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + i * kDxfN;
 #pragma unroll
           for (int c0 = 0; c0 < kDxfNt; c0 += 16) {
             uint32_t r1[16], r2[16];
@@ -1113,7 +1105,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
       if (!(vote[0] && vote[1] && vote[2] && vote[3])) break;
 #pragma unroll 1
       for (int i = 0; i < MSUB; ++i) {
-        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + i * kDxfNmma;
+        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_COLS + i * kDxfN;
         const float* xn = xs + (i * 4 + ((q + 1) & 3)) * 96;  // next quarter (q = 3: rows >= 126 only)
 #pragma unroll 1
         for (int c0 = 0; c0 < kDxfNt; c0 += 16) {
