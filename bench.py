@@ -490,6 +490,8 @@ def run_ours(args, rank, world, local):
                        "l2": "working set > L2 (net activations %.1f GB per step)" % (2 * k * 5.1e6 / 1e9),
                        "fp32_pairs_per_s": fp32,
                        "fp8_pairs_per_s": fp8,
+                       "fp8_note": "FP8 (E4M3 conv3-8) is outside the 1e-2 descriptor tolerance (~8e-2): "
+                                   "reported, not the headline",
                        "bf16_over_fp32": (value / fp32) if fp32 else None,
                        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                                       "n": len(lat)},
@@ -824,7 +826,7 @@ def run_batch(args, rank, world, local):
             _, _, grids = batch.describe(pd, off, vs, ks, seeds, kp_buf, desc_buf)
         stream = torch.cuda.current_stream()
         torch.cuda.synchronize()
-        if prec == "fp8":
+        if prec == "bf16":
             clocks = Clocks(local)
             clocks.start()
         l0 = tdm.launch_count()
@@ -835,7 +837,7 @@ def run_batch(args, rank, world, local):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
-        if prec == "fp8":
+        if prec == "bf16":
             clk = clocks.stop()
             launches = tdm.launch_count() - l0
         st = batch.stats()
@@ -854,27 +856,30 @@ def run_batch(args, rank, world, local):
     for prec in ("fp8", "bf16"):
         forms[prec]["rel_l2_vs_fp32_form"] = float(torch.linalg.norm(descs[prec].double() - ref) / torch.linalg.norm(ref))
     os.unlink(wfile)
-    ms8 = forms["fp8"]["ms_per_batch"]
-    achieved = K * NET_FLOP_PER_PATCH / ms8 / 1e9
+    # headline: the BF16 form (the form within the 1e-2 descriptor tolerance);
+    # FP8 (E4M3 conv3-8, ~8e-2 from the exact net) is reported beside it
+    ms16 = forms["bf16"]["ms_per_batch"]
+    achieved = K * NET_FLOP_PER_PATCH / ms16 / 1e9
     if rank == 0:
         print(json.dumps({
-            "metric": "batched fragments described/s (FP8 form)", "value": F * 1000.0 / ms8, "unit": "fragments/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms8, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "e4m3 (conv3-8) + bf16 (conv1-2, feat)",
+            "metric": "batched fragments described/s (BF16 form)", "value": F * 1000.0 / ms16, "unit": "fragments/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms16, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
             "data": "synthetic",
             "config": {"workload": "%d fragments of seeded rooms, %d..%d points (log-uniform), %d keypoints in total "
                                    "(uniform 500..5000 each), voxel 1 or 2 cm; TDF, keypoints, gather and the net "
                                    "as one replayed CUDA graph per batch" % (F, min(len(f[0]) for f in frags),
                                                                             max(len(f[0]) for f in frags), K),
                        "points": int(pts.shape[0]), "keypoints": K, "forms": forms,
-                       "fp8_over_fp32": forms["fp32"]["ms_per_batch"] / ms8,
+                       "fp8_note": "FP8 is outside the 1e-2 descriptor tolerance (E4M3 rounding, ~8e-2)",
+                       "fp8_over_fp32": forms["fp32"]["ms_per_batch"] / forms["fp8"]["ms_per_batch"],
                        "bf16_over_fp32": forms["fp32"]["ms_per_batch"] / forms["bf16"]["ms_per_batch"],
                        "l2": "working set > L2 (%.1f GB of grids)" % (forms["fp8"]["voxels"] * 6 / 1e9)},
             "roofline": {"kernel": "whole batch (net dominant)", "bound": "tensor", "achieved": achieved,
                          "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
                          "frac": achieved / peaks["bf16_tflops_sustained"],
                          "note": "useful net FLOPs per batch / batch time, against the measured BF16 sustained peak "
-                                 "(%s); E4M3 layers have twice the nominal BF16 rate" % kind},
+                                 "(%s); the batch runs about a second at full load" % kind},
             "clocks": clk, "gpu_launches": launches}))
     return 0
 
