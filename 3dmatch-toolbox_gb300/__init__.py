@@ -408,7 +408,7 @@ class Net:
         check(lib().tdm_net_tiles(self.handle, _ptr(nt), _ptr(ms)))
         return {k: (int(nt[i]), int(ms[i])) for i, k in enumerate(self.LAYER_SLOTS[:9])}
 
-    CONV_FORMS = ("grid", "dxf", "gather", "xrun", "gather_wt", "xrun_wt")
+    CONV_FORMS = ("grid", "dxf", "gather", "xrun", "gather_wt", "xrun_wt", "dxf_pair")
 
     def forms(self) -> dict:
         """{layer: kernel form}: "grid" (implicit GEMM over every input
@@ -416,7 +416,8 @@ class Net:
         valid output positions, A rows gathered per tap) or "xrun" (gathered
         (b, z, y) rows with whole input x runs, the dx taps sharing one operand);
         "gather_wt" / "xrun_wt" put the weights in the MMA's A operand (conv3,
-        conv4)."""
+        conv4); "dxf_pair" runs conv2's dx-fused form on CTA pairs sharing each
+        MMA (M = 256, N = 192)."""
         f = np.zeros(9, np.int32)
         check(lib().tdm_net_tile_forms(self.handle, _ptr(f)))
         return {k: self.CONV_FORMS[int(f[i])] for i, k in enumerate(self.LAYER_SLOTS[:9])}

@@ -33,6 +33,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <mutex>
 #include <cstring>
 #include <vector>
@@ -74,6 +75,24 @@ __host__ __device__ constexpr uint32_t tmem_cols_for(int c) {
 }
 
 __device__ __forceinline__ bool aborted(const int* err) { return *reinterpret_cast<const volatile int*>(err) != 0; }
+
+// wait_or_flag for barriers the other CTA of a pair arrives on (acquire at
+// cluster scope).
+__device__ __forceinline__ bool wait_or_flag_cluster(uint32_t bar, uint32_t parity, int* err, int code) {
+  if (ptx::mbar_try_wait_cluster(bar, parity)) return true;
+  uint64_t t0 = ptx::globaltimer_ns();
+  uint32_t spins = 0;
+  while (true) {
+    if (ptx::mbar_try_wait_cluster(bar, parity)) return true;
+    if ((++spins & 255u) == 0) {
+      if (aborted(err)) return false;
+      if (ptx::globaltimer_ns() - t0 > kWaitBudgetNs) {
+        atomicCAS(err, 0, code);
+        return false;
+      }
+    }
+  }
+}
 
 // Waits for phase `parity` of `bar`.  Gives up (false) when another role of
 // the kernel has raised the error word, or after budget_ns of wall time, when
@@ -1231,6 +1250,363 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
 }
 
 // ---------------------------------------------------------------------------
+// conv2 on a CTA pair (cta_group::2).
+//
+// The dx-fused kernel above issues one N = 96 MMA (three dx taps x 32 output
+// channels) per 128 rows and K step.  Such an MMA reads 7 KB of operands for
+// 48 cycles of math, so it keeps the SM's shared-memory read port busy on its
+// own (56 cycles alone), and the kernel's other shared-memory traffic (slab
+// copies, output staging) stretches it further.  Here the two CTAs of a
+// cluster share each MMA (tcgen05.mma.cta_group::2): M = 256 rows -- 128 from
+// each CTA's slab -- by N = 192 columns, the three dx taps of all 64 output
+// channels, whose weights are split between the CTAs exactly as the resident
+// halves above (the leader's 110.6 KB give channels 0..31, the peer's
+// 32..63).  Each SM still reads 7 KB per MMA, now for 96 cycles of math.
+//
+// A pair tile is 252 output rows: the leader computes MMA rows [m0, m0 + 128)
+// and stores outputs [m0, m0 + 126), the peer [m0 + 126, ...).  Roles:
+//   warp 0, lane 0 (both CTAs): weights once, then its own A slabs (three dz
+//     stages per tile) by bulk copies on its own barriers;
+//   warp 1, lane 0: the leader issues every MMA and commits with multicast to
+//     both CTAs' barriers (stage free, accumulator full); the peer relays its
+//     own "weights landed" and "slab landed" completions to the leader by
+//     remote mbarrier arrives;
+//   warps 2-9 (both CTAs): two epilogue sets, set h draining the 96 columns of
+//     channel half h for the CTA's 128 TMEM lanes (the dx row-shift sum of the
+//     kernel above), then signalling the
+//     leader's accumulator-empty barrier (eight local and eight remote
+//     arrivals).
+// TMEM: one pair allocation (issued together by warp 1 of both CTAs), two
+// accumulator buffers of 192 columns.  Every mbarrier wait is bounded; both
+// CTAs always reach the cluster barriers (no early exit), so a timeout in one
+// CTA makes the other's waits run out too, and both free their TMEM.
+// The sums are the kernel above's in the same order, so the outputs are the
+// same bits.
+// ---------------------------------------------------------------------------
+constexpr int kD2Threads = 320;
+constexpr int kD2NSA = 3;                 // A slab stages per CTA
+constexpr int kD2N = 2 * kDxfN;           // 192 accumulator columns per buffer
+constexpr int kD2Out = 2 * kDxfSub;       // 252 output rows per pair tile
+constexpr uint32_t kD2Xchg = 2u * 2u * 4u * 96u * 4u;  // [set][parity][quarter][P1 l0, P2 l0, P2 l1] x 32
+constexpr uint32_t kD2Stage = 8u * 128u * 16u;         // output staging [chunk][row][16 B]
+constexpr int kD2Bars = 3 * kD2NSA + 7;
+
+__device__ __forceinline__ void epi_bar_set(int set) {
+  if (set == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
+  else asm volatile("bar.sync 2, 128;" ::: "memory");
+}
+
+template <bool FP8_OUT, bool XPOOL>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_conv_dxf2_kernel(const KParams p) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t TMEM_COLS = 512;
+  const int R = p.R;
+  const uint32_t a_stage = 16u * 8u * (uint32_t)R;
+  uint8_t* sW = smem;
+  uint8_t* sA = smem + kDxfWBytes;
+  float* sX = reinterpret_cast<float*>(sA + kD2NSA * a_stage);
+  uint8_t* sO = reinterpret_cast<uint8_t*>(sX) + kD2Xchg;
+  int* sVote = reinterpret_cast<int*>(sO + kD2Stage);  // [set][parity][quarter]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sVote + 16);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + kD2Bars);
+
+  const uint32_t rank = ptx::cluster_rank();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // a CTA that starts with the error word raised skips its loops but still
+  // meets its peer at both cluster barriers
+  const bool skip = !__syncthreads_and(aborted(p.err) ? 0 : 1);
+
+  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * kD2NSA, peerA = emptyA + 8 * kD2NSA;
+  const uint32_t wfull = peerA + 8 * kD2NSA, peerW = wfull + 8, accFull = peerW + 8, accEmpty = accFull + 16,
+                 done = accEmpty + 16;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kD2NSA; ++i) {
+      ptx::mbar_init(fullA + 8 * i, 1);
+      ptx::mbar_init(emptyA + 8 * i, 1);
+      ptx::mbar_init(peerA + 8 * i, 1);
+    }
+    ptx::mbar_init(wfull, 1);
+    ptx::mbar_init(peerW, 1);
+    for (int i = 0; i < 2; ++i) {
+      ptx::mbar_init(accFull + 8 * i, 1);
+      ptx::mbar_init(accEmpty + 8 * i, 16);  // 8 epilogue warps here, 8 in the peer
+    }
+    ptx::mbar_init(done, 1);
+    ptx::fence_barrier_init();
+    ptx::fence_proxy_async_smem();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc2(ptx::smem_u32(tmem_holder), TMEM_COLS);
+    ptx::tmem_relinquish2();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::cluster_sync();  // both CTAs' barriers exist before any remote arrive or multicast commit
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  const uint32_t sA_u = ptx::smem_u32(sA), sW_u = ptx::smem_u32(sW);
+  const int64_t plane = (int64_t)p.D * p.D;
+  const int64_t pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
+
+  if (warp == 0) {
+    if (lane == 0 && !skip) {
+      // ---------------- producer: this CTA's weight half once, then its A slabs ----------------
+      ptx::mbar_arrive_expect_tx(wfull, kDxfWBytes);
+      for (int b = 0; b < 9; ++b)
+        ptx::bulk_g2s(sW_u + b * kDxfBlock, p.wpk + (size_t)rank * kDxfWBytes + (size_t)b * kDxfBlock, kDxfBlock,
+                      wfull);
+      int sa = 0;
+      uint32_t pha = 0;
+      int armedA[kD2NSA];
+      for (int i = 0; i < kD2NSA; ++i) armedA[i] = -1;
+      bool ok = true;
+      for (int64_t t = pair; t < p.total_tiles && ok; t += npairs) {
+        const int64_t m0 = t * kD2Out;
+        if (!tile_has_work(p, m0, kD2Out)) continue;
+        const int64_t s0 = m0 + (int64_t)rank * kDxfSub;
+        for (int zt = 0; zt < 3; ++zt) {
+          if (!TDM_TIMED_WAIT(3, wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
+          ptx::mbar_arrive_expect_tx(fullA + 8 * sa, a_stage);
+          armedA[sa] = (int)pha;
+          const uint8_t* src = p.act + (s0 + zt * plane) * 16;
+          for (int j = 0; j < 8; ++j)
+            ptx::bulk_g2s(sA_u + sa * a_stage + j * R * 16, src + j * p.act_cs, R * 16, fullA + 8 * sa);
+          if (++sa == kD2NSA) { sa = 0; pha ^= 1; }
+        }
+      }
+      for (int i = 0; i < kD2NSA; ++i)
+        if (armedA[i] >= 0) wait_or_flag(fullA + 8 * i, (uint32_t)armedA[i], p.err, DEV_TIMEOUT_PRODUCER);
+      wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_PRODUCER);
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && !skip && rank == 1) {
+      // ---------------- peer: relay its copy completions to the leader ----------------
+      bool ok = wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_PRODUCER);
+      if (ok) ptx::mbar_arrive_remote(peerW, 0);
+      int sa = 0;
+      uint32_t pha = 0;
+      for (int64_t t = pair; t < p.total_tiles && ok; t += npairs) {
+        const int64_t m0 = t * kD2Out;
+        if (!tile_has_work(p, m0, kD2Out)) continue;
+        for (int zt = 0; zt < 3; ++zt) {
+          if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+          ptx::mbar_arrive_remote(peerA + 8 * sa, 0);
+          if (++sa == kD2NSA) { sa = 0; pha ^= 1; }
+        }
+      }
+    } else if (lane == 0 && !skip && rank == 0) {
+      // ---------------- leader: the pair's MMA issuer ----------------
+      constexpr uint32_t idesc = ptx::make_idesc(kD2N, 256, 1, 1);
+      const uint32_t lboA = (uint32_t)R * 16u;
+      const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), wDesc0 = ptx::smem_desc(sW_u, kDxfN * 16, 128);
+      bool ok = wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_MMA) &&
+                wait_or_flag_cluster(peerW, 0, p.err, DEV_TIMEOUT_MMA);
+      int sa = 0;
+      uint32_t pha = 0, j = 0;
+#ifdef TDM_WAIT_STATS
+      const long long t_loop0 = clock64();
+#endif
+      for (int64_t t = pair; t < p.total_tiles && ok; t += npairs) {
+        const int64_t m0 = t * kD2Out;
+        if (!tile_has_work(p, m0, kD2Out)) continue;
+        const uint32_t buf = j & 1u, use = j >> 1;
+        if (!TDM_TIMED_WAIT(0, wait_or_flag_cluster(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
+        ptx::tc_fence_after();
+        const uint32_t dbase = tmem + buf * kD2N;
+        uint32_t accumulate = 0;
+        for (int zt = 0; zt < 3 && ok; ++zt) {
+          if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA)) ||
+              !TDM_TIMED_WAIT(2, wait_or_flag_cluster(peerA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) {
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          const uint64_t aStage = ptx::desc_advance(aDesc0, sa * a_stage);
+#pragma unroll
+          for (int dy = 0; dy < 3; ++dy) {
+            const uint64_t aRow = ptx::desc_advance(aStage, (uint32_t)(dy * p.D) * 16u);
+            const uint64_t wDesc = ptx::desc_advance(wDesc0, (uint32_t)(zt * 3 + dy) * kDxfBlock);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              ptx::mma2_f16(dbase, ptx::desc_advance(aRow, (2 * kk) * lboA),
+                            ptx::desc_advance(wDesc, (2 * kk) * kDxfN * 16), idesc, accumulate);
+              accumulate = 1;
+            }
+          }
+          ptx::mma2_commit_both(emptyA + 8 * sa);
+          if (++sa == kD2NSA) { sa = 0; pha ^= 1; }
+        }
+        if (!ok) break;
+        ptx::mma2_commit_both(accFull + 8 * buf);
+        ++j;
+      }
+#ifdef TDM_WAIT_STATS
+      atomicAdd(&g_wait_stats[6], (unsigned long long)(clock64() - t_loop0));
+#endif
+      ptx::mma2_commit_both(done);
+      wait_or_flag(done, 0, p.err, DEV_TIMEOUT_MMA);
+    }
+  } else if (!skip) {
+    // ---------------- epilogue: set h = channel half h, TMEM lane quarter q = warp % 4 ----------------
+    const int set = (warp - 2) >> 2;
+    const uint32_t sO_u = ptx::smem_u32(sO);
+    constexpr int CH = FP8_OUT ? 2 : 4;  // 16-byte output chunks of this set's 32 channels
+    const int q = warp & 3;
+    const int L = q * 32 + lane;  // TMEM lane = row within the CTA's 128 rows
+    const int n0 = set * kDxfNt;  // first output channel of this set
+    bool issued = false;
+    uint32_t j = 0;
+    for (int64_t t = pair; t < p.total_tiles; t += npairs) {
+      const int64_t m0 = t * kD2Out;
+      if (!tile_has_work(p, m0, kD2Out)) continue;
+      const uint32_t buf = j & 1u, use = j >> 1;
+      const int got = __all_sync(
+          0xffffffffu, TDM_TIMED_WAIT(5, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE)) ? 1 : 0);
+      int* vote = sVote + (set * 2 + (j & 1u)) * 4;
+      if (lane == 0) vote[q] = got;
+      // exchange: the previous quarter's lanes 30 and 31 need this quarter's
+      // lane 0 (P1, P2) and lane 1 (P2) values (rows +1 and +2 cross the
+      // 32-lane boundary); published before barrier A
+      float* xs = sX + (set * 2 + (j & 1u)) * (4 * 96);
+      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * kD2N + set * kDxfN;
+      if (got) {
+        ptx::tc_fence_after();
+#pragma unroll
+        for (int c0 = 0; c0 < kDxfNt; c0 += 16) {
+          uint32_t r1[16], r2[16];
+          ptx::tmem_ld16_nowait(ta + kDxfNt + c0, r1);
+          ptx::tmem_ld16_nowait(ta + 2 * kDxfNt + c0, r2);
+          ptx::tmem_wait_ld();
+          float* xw = xs + q * 96;
+          if (lane == 0) {
+#pragma unroll
+            for (int e = 0; e < 16; ++e) { xw[c0 + e] = __uint_as_float(r1[e]); xw[32 + c0 + e] = __uint_as_float(r2[e]); }
+          } else if (lane == 1) {
+#pragma unroll
+            for (int e = 0; e < 16; ++e) xw[64 + c0 + e] = __uint_as_float(r2[e]);
+          }
+        }
+      }
+      if (issued) ptx::bulk_wait_read_all();  // the staging area is free again
+      epi_bar_set(set);  // A
+      if (!(vote[0] && vote[1] && vote[2] && vote[3])) break;
+      const float* xn = xs + ((q + 1) & 3) * 96;  // next quarter (q = 3: rows >= 126 only)
+#pragma unroll 1
+      for (int c0 = 0; c0 < kDxfNt; c0 += 16) {
+        uint32_t r0[16], r1[16], r2[16];
+        ptx::tmem_ld16_nowait(ta + c0, r0);
+        ptx::tmem_ld16_nowait(ta + kDxfNt + c0, r1);
+        ptx::tmem_ld16_nowait(ta + 2 * kDxfNt + c0, r2);
+        ptx::tmem_wait_ld();
+        float nb1[16], nb2a[16], nb2b[16], bi[16];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float4 u = reinterpret_cast<const float4*>(xn + c0)[k];
+          const float4 w = reinterpret_cast<const float4*>(xn + 32 + c0)[k];
+          const float4 z = reinterpret_cast<const float4*>(xn + 64 + c0)[k];
+          const float4 c = __ldg(reinterpret_cast<const float4*>(p.bias + n0 + c0) + k);
+          nb1[4 * k] = u.x; nb1[4 * k + 1] = u.y; nb1[4 * k + 2] = u.z; nb1[4 * k + 3] = u.w;
+          nb2a[4 * k] = w.x; nb2a[4 * k + 1] = w.y; nb2a[4 * k + 2] = w.z; nb2a[4 * k + 3] = w.w;
+          nb2b[4 * k] = z.x; nb2b[4 * k + 1] = z.y; nb2b[4 * k + 2] = z.z; nb2b[4 * k + 3] = z.w;
+          bi[4 * k] = c.x; bi[4 * k + 1] = c.y; bi[4 * k + 2] = c.z; bi[4 * k + 3] = c.w;
+        }
+        const bool l31 = lane == 31, l30 = lane == 30;
+        float v[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          float s1 = __shfl_down_sync(0xffffffffu, __uint_as_float(r1[e]), 1);
+          float s2 = __shfl_down_sync(0xffffffffu, __uint_as_float(r2[e]), 2);
+          s1 = l31 ? nb1[e] : s1;
+          s2 = l31 ? nb2b[e] : (l30 ? nb2a[e] : s2);
+          const float a = ((__uint_as_float(r0[e]) + s1) + s2) + bi[e];
+          v[e] = p.relu ? fmaxf(a, 0.0f) : a;
+        }
+        const bool stage = !XPOOL || (L & 1) == 0;
+        const int SL = XPOOL ? (L >> 1) : L;
+        if (FP8_OUT) {
+          uint4 o;
+          o.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
+          o.y = pack_e4m3x4(v[4] * p.out_qinv, v[5] * p.out_qinv, v[6] * p.out_qinv, v[7] * p.out_qinv);
+          o.z = pack_e4m3x4(v[8] * p.out_qinv, v[9] * p.out_qinv, v[10] * p.out_qinv, v[11] * p.out_qinv);
+          o.w = pack_e4m3x4(v[12] * p.out_qinv, v[13] * p.out_qinv, v[14] * p.out_qinv, v[15] * p.out_qinv);
+          if (XPOOL) {
+            o.x = __vmaxu4(o.x, __shfl_xor_sync(0xffffffffu, o.x, 1));
+            o.y = __vmaxu4(o.y, __shfl_xor_sync(0xffffffffu, o.y, 1));
+            o.z = __vmaxu4(o.z, __shfl_xor_sync(0xffffffffu, o.z, 1));
+            o.w = __vmaxu4(o.w, __shfl_xor_sync(0xffffffffu, o.w, 1));
+          }
+          if (stage) *reinterpret_cast<uint4*>(sO + ((set * CH + c0 / 16) * 128 + SL) * 16) = o;
+        } else {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            uint4 o;
+            o.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
+            o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
+            o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
+            o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
+            if (XPOOL) {
+              uint32_t* w = reinterpret_cast<uint32_t*>(&o);
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                const uint32_t nb = __shfl_xor_sync(0xffffffffu, w[k], 1);
+                __nv_bfloat162 m = __hmax2(*reinterpret_cast<const __nv_bfloat162*>(&w[k]),
+                                           *reinterpret_cast<const __nv_bfloat162*>(&nb));
+                w[k] = *reinterpret_cast<uint32_t*>(&m);
+              }
+            }
+            if (stage) *reinterpret_cast<uint4*>(sO + ((set * CH + c0 / 8 + h) * 128 + SL) * 16) = o;
+          }
+        }
+      }
+      ptx::tc_fence_before();
+      ptx::fence_proxy_async_smem();  // staging writes visible to the bulk copies
+      epi_bar_set(set);               // B
+      if (lane == 0) {
+        if (rank == 0) mbar_arrive(accEmpty + 8 * buf);
+        else ptx::mbar_arrive_remote(accEmpty + 8 * buf, 0);
+      }
+      // output runs of this CTA's 126 rows: lane k of quarter 0 takes the k-th
+      // grid row (b, z, y) they touch, for this set's chunks
+      if (q == 0) {
+        const int64_t s0 = m0 + (int64_t)rank * kDxfSub;
+        const int64_t e0 = min(s0 + kDxfSub, p.rows);
+        const int64_t y0 = s0 / p.D;
+        const int64_t yr = y0 + lane;  // grid row index (b*D + z)*D + y
+        const int64_t ra = max(s0, yr * p.D), rb = min(e0, yr * p.D + p.Do);
+        if (lane < 6 && ra < rb) {
+          const int64_t bz = yr / p.D;
+          const int y = (int)(yr - bz * p.D);
+          const int64_t b = bz / p.D;
+          const int z = (int)(bz - b * p.D);
+          if (y < p.Do && z < p.Do) {
+            const int x = (int)(ra - yr * p.D);
+            const int XO = XPOOL ? p.Do / 2 : p.Do;
+            const int64_t pout = ((b * p.Do + z) * p.Do + y) * XO + (XPOOL ? x / 2 : x);
+            const uint32_t len = (uint32_t)((rb - ra) / (XPOOL ? 2 : 1)) * 16u;
+            const int srow = (int)(ra - s0) / (XPOOL ? 2 : 1);
+#pragma unroll
+            for (int c = 0; c < CH; ++c)
+              ptx::bulk_s2g(p.out + (int64_t)(n0 / (FP8_OUT ? 16 : 8) + c) * p.out_cs + pout * 16,
+                            sO_u + ((set * CH + c) * 128 + srow) * 16, len);
+            ptx::bulk_commit();
+            issued = true;
+          }
+        }
+      }
+      ++j;
+    }
+    if (issued) ptx::bulk_wait_all();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::cluster_sync();  // the pair's MMAs are done and both CTAs have read their accumulators
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc2(tmem, TMEM_COLS);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // conv1 with the im2col operand built in shared memory.  conv1 (1 input
 // channel, 27 taps) is a GEMM over the 28^3 output positions of each patch
 // with K = 27 taps padded to 32 and N = 64.  Instead of writing that operand
@@ -1429,6 +1805,9 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
   }
 }
 
+// A slab rows per CTA of the pair form: its 128 MMA rows shifted by up to 2 D
+int pair_slab_rows(const TcLayer& L) { return 128 + 2 * L.D; }
+
 int slab_rows(const TcLayer& L) {
   if (L.dxf) return (L.msub - 1) * kDxfSub + 128 + 2 * L.D;  // exact: the stages must fit beside the weights
   int r = L.msub * 128 + (L.nyx > 1 ? 2 * L.D + 2 : 0);
@@ -1472,6 +1851,8 @@ int weight_stages(const TcLayer& L) {
 }
 
 size_t smem_bytes(const TcLayer& L) {
+  if (L.dxf && L.pair)
+    return kDxfWBytes + (size_t)kD2NSA * 16 * 8 * pair_slab_rows(L) + kD2Xchg + kD2Stage + 64 + kSmemReserve;
   if (L.dxf) return kDxfWBytes + kDxfNSA * a_stage_bytes(L) + kDxfXchg + kDxfStage + 32 + kSmemReserve;
   if (L.gather)
     return gather_stages(L) * gather_stage_bytes(L) + (L.wt ? kWtStage : 0) + (size_t)weight_stages(L) * L.nt * 128 +
@@ -1560,6 +1941,49 @@ bool gather_tile_built(int nt, int msub) {
   return (nt == 256 && (msub == 1 || msub == 2)) || (nt == 128 && msub == 2);
 }
 
+// CTA pairs of the pair form that can be resident at once on this device
+// (clusters need both CTAs on one GPC; one CTA per SM), cached per device.
+template <bool FP8_OUT, bool XPOOL>
+int dxf2_max_pairs(size_t smem) {
+  static std::mutex mu;
+  static std::map<int, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2 * (unsigned)(device_sm_count() / 2), 1, 1);
+  cfg.blockDim = dim3(kD2Threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, tc_conv_dxf2_kernel<FP8_OUT, XPOOL>, &cfg) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    n = device_sm_count() / 2;
+  }
+  cache[dev] = n;
+  return n;
+}
+
+template <bool FP8_OUT, bool XPOOL>
+tdm_status launch_dxf2(const KParams& kp, size_t smem, cudaStream_t s) {
+  auto kern = tc_conv_dxf2_kernel<FP8_OUT, XPOOL>;
+  cudaError_t attr_err = raise_smem_cap(reinterpret_cast<const void*>(kern), (int)kSmemLimit);
+  if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_dxf2_kernel)");
+  // persistent: no more pairs than fit at once, so every pair runs from the start
+  const int64_t pairs = std::max<int64_t>(1, std::min<int64_t>(kp.total_tiles, dxf2_max_pairs<FP8_OUT, XPOOL>(smem)));
+  kern<<<(unsigned)(2 * pairs), kD2Threads, smem, s>>>(kp);
+  TDM_CHECK_LAUNCH("tc_conv_dxf2_kernel");
+  return TDM_OK;
+}
+
 template <int MSUB, bool FP8_OUT, bool XPOOL>
 tdm_status launch_dxf(const KParams& kp, size_t smem, cudaStream_t s) {
   auto kern = tc_conv_dxf_kernel<MSUB, FP8_OUT, XPOOL>;
@@ -1627,6 +2051,9 @@ int64_t tc_tail_rows(const TcLayer& L) {
 }
 
 bool tc_layer_fits(const TcLayer& L) {
+  if (L.dxf && L.pair)  // the pair covers both channel halves and 2 x 126 rows: tile (32, 2) only
+    return L.nt == kDxfNt && L.msub == 2 && L.cin == 64 && L.cout == 2 * kDxfNt && L.nz == 3 && L.nyx == 9 &&
+           !L.fp8_in && smem_bytes(L) <= kSmemLimit;
   if (L.dxf)
     return L.nt == kDxfNt && (L.msub == 1 || L.msub == 2) && L.cin == 64 && L.cout == 2 * kDxfNt && L.nz == 3 &&
            L.nyx == 9 && !L.fp8_in && smem_bytes(L) <= kSmemLimit;
@@ -1662,6 +2089,22 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   kp.R = slab_rows(L);
   kp.err = device_error_word();
   if (!kp.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
+  if (L.dxf && L.pair) {
+    TDM_REQUIRE(tc_layer_fits(L), "tc layer: unsupported dx-fused pair tile");
+    TDM_REQUIRE((reinterpret_cast<uintptr_t>(a.act) & 15) == 0 && (a.act_cs & 15) == 0 &&
+                    (reinterpret_cast<uintptr_t>(L.wpk) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.out) & 15) == 0 &&
+                    (a.out_cs & 15) == 0,
+                "tc layer: operands must be 16-byte aligned");
+    if (a.rows == 0) return TDM_OK;
+    TDM_REQUIRE(!a.xpool || (L.D % 2 == 0 && L.Do % 2 == 0), "tc layer: x-pooled output needs even extents");
+    kp.R = pair_slab_rows(L);
+    kp.ntiles = 1;
+    kp.nsb = 0;
+    kp.total_tiles = (a.rows + kD2Out - 1) / kD2Out;
+    const size_t smem = smem_bytes(L);
+    if (L.fp8_out) return a.xpool ? launch_dxf2<true, true>(kp, smem, s) : launch_dxf2<true, false>(kp, smem, s);
+    return a.xpool ? launch_dxf2<false, true>(kp, smem, s) : launch_dxf2<false, false>(kp, smem, s);
+  }
   if (L.dxf) {
     TDM_REQUIRE(tc_layer_fits(L), "tc layer: unsupported dx-fused tile");
     TDM_REQUIRE((reinterpret_cast<uintptr_t>(a.act) & 15) == 0 && (a.act_cs & 15) == 0 &&

@@ -49,6 +49,9 @@ struct TcLayer {
   // two rows; nt = 32 output channels per CTA (two halves), weights resident
   // in shared memory, msub sub-tiles of 128 rows giving 126 outputs each.
   bool dxf = false;
+  // dx-fused on a CTA pair (cta_group::2): one M = 256, N = 192 MMA per K step
+  // covers 256 rows and all 64 output channels (each CTA holds one weight half)
+  bool pair = false;
   // gathered-row form (3x3x3 convs): M runs over the valid output positions
   // only and gather warps copy each tap's A rows into shared memory, instead
   // of the grid form's rows for every input position.

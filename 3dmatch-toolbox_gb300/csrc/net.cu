@@ -201,8 +201,9 @@ TcLayer make_tc_layer(int l, bool use_feat) {
   if (L.cout == 64) { L.nt = 64; L.msub = 4; }
   else if (L.cout == 128) { L.nt = 128; L.msub = 2; }
   else { L.nt = 256; L.msub = 1; }
-  if (l == 1) {  // conv2: the dx taps share one N = 96 MMA per half of the outputs
+  if (l == 1) {  // conv2: the dx taps share one MMA; a CTA pair covers both halves of the outputs
     L.dxf = true;
+    L.pair = true;
     L.nt = 32;
     L.msub = 2;
   }
@@ -714,7 +715,7 @@ bool form_xrun(int f) { return f == TDM_CONV_XRUN || f == TDM_CONV_XRUN_WT; }
 bool form_wt(int f) { return f == TDM_CONV_GATHER_WT || f == TDM_CONV_XRUN_WT; }
 
 int form_of(const TcLayer& L) {
-  if (L.dxf) return TDM_CONV_DXF;
+  if (L.dxf) return L.pair ? TDM_CONV_DXF_PAIR : TDM_CONV_DXF;
   if (!L.gather) return TDM_CONV_GRID;
   if (L.wt) return L.xrun ? TDM_CONV_XRUN_WT : TDM_CONV_GATHER_WT;
   return L.xrun ? TDM_CONV_XRUN : TDM_CONV_GATHER;
@@ -729,10 +730,14 @@ TcLayer& active_layer(tdm_net* net, int l) {
 // im2col GEMM has one weight packing (N = 64).
 std::vector<Tile> tile_candidates(tdm_net* net, int l) {
   std::vector<Tile> out;
-  if (active_layer(net, l).dxf) {  // the dx-fused conv2: 32 channels per CTA, 1 or 2 sub-tiles
+  if (active_layer(net, l).dxf) {  // the dx-fused conv2: on a CTA pair, or 32 channels per CTA
+    TcLayer L = active_layer(net, l);
+    L.msub = 2;
+    L.pair = true;
+    if (tc_layer_fits(L)) out.push_back(Tile{32, 2, TDM_CONV_DXF_PAIR});
     for (int ms : {2, 1}) {
-      TcLayer L = active_layer(net, l);
       L.msub = ms;
+      L.pair = false;
       if (tc_layer_fits(L)) out.push_back(Tile{32, ms, TDM_CONV_DXF});
     }
     return out;
@@ -777,7 +782,9 @@ tdm_status set_tile(tdm_net* net, int l, Tile t) {
   if (L.nt != t.nt || L.msub != t.msub || form_of(L) != t.form) ++net->generation;
   L.nt = t.nt;
   L.msub = t.msub;
-  if (!L.dxf) {
+  if (L.dxf) {
+    L.pair = t.form == TDM_CONV_DXF_PAIR;
+  } else {
     L.gather = form_gathers(t.form);
     L.xrun = form_xrun(t.form);
     L.wt = form_wt(t.form);

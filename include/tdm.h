@@ -176,14 +176,17 @@ tdm_status tdm_net_set_tile(tdm_net* net, int32_t layer, int32_t nt, int32_t msu
  * x runs, one staged operand shared by the three dx taps (same layers and
  * tiles); GATHER_WT / XRUN_WT: the same with the weights as the MMA's A
  * operand (M = 128 output channels, N = 256 rows; conv3 and conv4, tile
- * (128,2)).  All forms give the same bits. */
+ * (128,2)); DXF_PAIR: conv2's dx-fused form on a pair of CTAs sharing each
+ * MMA (M = 256 rows, N = 192: the dx taps of all 64 channels; tile (32,2)).
+ * All forms give the same bits. */
 typedef enum {
   TDM_CONV_GRID = 0,
   TDM_CONV_DXF = 1,
   TDM_CONV_GATHER = 2,
   TDM_CONV_XRUN = 3,
   TDM_CONV_GATHER_WT = 4,
-  TDM_CONV_XRUN_WT = 5
+  TDM_CONV_XRUN_WT = 5,
+  TDM_CONV_DXF_PAIR = 6
 } tdm_conv_form;
 tdm_status tdm_net_tile_forms(const tdm_net* net, int32_t form[9]);
 /* Sets tile and form (-1: the current form if it has the tile, else any). */

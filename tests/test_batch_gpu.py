@@ -141,8 +141,8 @@ def test_autotune_keeps_descriptor_bits(tdm, weights, patches, precision):
     tiles = net.autotune(patches, reps=2)
     forms = net.forms()
     for layer, (nt, ms) in tiles.items():
-        if layer == "conv2":  # dx-fused: 32 outputs per CTA, N = 96
-            assert forms[layer] == "dxf" and nt == 32 and ms in (1, 2), layer
+        if layer == "conv2":  # dx-fused: on a CTA pair (N = 192), or 32 outputs per CTA (N = 96)
+            assert forms[layer] in ("dxf", "dxf_pair") and nt == 32 and ms in (1, 2), layer
         elif forms[layer] in ("gather", "xrun", "gather_wt", "xrun_wt"):  # one accumulator buffer allowed
             assert layer in ("conv3", "conv4", "conv5", "conv6", "conv7"), layer
             assert (nt, ms) in ((256, 2), (256, 1), (128, 2)), layer
@@ -154,7 +154,7 @@ def test_autotune_keeps_descriptor_bits(tdm, weights, patches, precision):
     tdm.device_status()
 
 
-@pytest.mark.parametrize("layer,tiles", [("conv2", [(32, 2), (32, 1)]),
+@pytest.mark.parametrize("layer,tiles", [("conv2", [(32, 2, "dxf"), (32, 1, "dxf"), (32, 2, "dxf_pair")]),
                                          ("conv3", [(64, 4), (64, 2), (128, 2), (128, 1), (128, 2, "gather"),
                                                     (128, 2, "xrun"), (128, 2, "gather_wt"), (128, 2, "xrun_wt")]),
                                          ("conv4", [(128, 2, "gather"), (128, 2, "grid"), (128, 2, "xrun"),
@@ -222,4 +222,32 @@ def test_gathered_forms_small_batches(tdm, weights, patches, precision):
         for lo, hi in ((7, 8), (0, 3), (100, 137)):
             got = net.forward(patches[lo:hi].contiguous()).cpu().numpy()
             assert np.array_equal(got, full[lo:hi]), (form, lo, hi)
+    tdm.device_status()
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp8"])
+def test_conv2_pair_form_same_bits(tdm, weights, patches, precision):
+    """conv2 on a CTA pair (one M = 256, N = 192 MMA over two SMs) against the
+    single-CTA dx-fused form: the same descriptor, conv2 (unfused epilogue)
+    and pool1 (x-pair max in the epilogue) bits, on full, tiny and ragged
+    batches (tiles that straddle patches, the pair's second half past the
+    last row)."""
+    net = tdm.Net(weights, precision=precision)
+    if precision == "fp8":
+        net.calibrate(patches)
+    assert net.forms()["conv2"] == "dxf_pair"  # the default
+    out = {}
+    for form, ms in (("dxf_pair", 2), ("dxf", 2), ("dxf", 1)):
+        net.set_tile("conv2", 32, ms, form)
+        assert net.forms()["conv2"] == form
+        for lo, hi in ((0, 300), (7, 8), (0, 3), (100, 137)):
+            b = patches[lo:hi].contiguous()
+            out[(form, ms, lo, hi, "desc")] = net.forward(b).cpu().numpy()
+            if hi - lo <= 37:
+                out[(form, ms, lo, hi, "conv2")] = net.response("conv2", b).cpu().numpy()
+                out[(form, ms, lo, hi, "pool1")] = net.response("pool1", b).cpu().numpy()
+    for key, v in out.items():
+        if key[0] != "dxf_pair":
+            ref = out[("dxf_pair", 2) + key[2:]]
+            assert np.array_equal(v, ref), key
     tdm.device_status()
