@@ -1460,8 +1460,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       const int64_t m0 = t * kD2Out;
       if (!tile_has_work(p, m0, kD2Out)) continue;
       const uint32_t buf = j & 1u, use = j >> 1;
-      const int got = __all_sync(
-          0xffffffffu, TDM_TIMED_WAIT(5, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE)) ? 1 : 0);
+#ifdef TDM_WAIT_STATS
+      const long long c_w = clock64();
+#endif
+      const int got = __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0);
+#ifdef TDM_WAIT_STATS
+      if (lane == 0) atomicAdd(&g_wait_stats[5], (unsigned long long)(clock64() - c_w));
+#endif
       int* vote = sVote + (set * 2 + (j & 1u)) * 4;
       if (lane == 0) vote[q] = got;
       // exchange: the previous quarter's lanes 30 and 31 need this quarter's
@@ -1471,19 +1476,27 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * kD2N + set * kDxfN;
       if (got) {
         ptx::tc_fence_after();
+        // all four loads in flight before one wait
+        uint32_t r1a[16], r2a[16], r1b[16], r2b[16];
+        ptx::tmem_ld16_nowait(ta + kDxfNt, r1a);
+        ptx::tmem_ld16_nowait(ta + 2 * kDxfNt, r2a);
+        ptx::tmem_ld16_nowait(ta + kDxfNt + 16, r1b);
+        ptx::tmem_ld16_nowait(ta + 2 * kDxfNt + 16, r2b);
+        ptx::tmem_wait_ld();
+        float* xw = xs + q * 96;
+        if (lane == 0) {
 #pragma unroll
-        for (int c0 = 0; c0 < kDxfNt; c0 += 16) {
-          uint32_t r1[16], r2[16];
-          ptx::tmem_ld16_nowait(ta + kDxfNt + c0, r1);
-          ptx::tmem_ld16_nowait(ta + 2 * kDxfNt + c0, r2);
-          ptx::tmem_wait_ld();
-          float* xw = xs + q * 96;
-          if (lane == 0) {
+          for (int e = 0; e < 16; ++e) {
+            xw[e] = __uint_as_float(r1a[e]);
+            xw[16 + e] = __uint_as_float(r1b[e]);
+            xw[32 + e] = __uint_as_float(r2a[e]);
+            xw[48 + e] = __uint_as_float(r2b[e]);
+          }
+        } else if (lane == 1) {
 #pragma unroll
-            for (int e = 0; e < 16; ++e) { xw[c0 + e] = __uint_as_float(r1[e]); xw[32 + c0 + e] = __uint_as_float(r2[e]); }
-          } else if (lane == 1) {
-#pragma unroll
-            for (int e = 0; e < 16; ++e) xw[64 + c0 + e] = __uint_as_float(r2[e]);
+          for (int e = 0; e < 16; ++e) {
+            xw[64 + e] = __uint_as_float(r2a[e]);
+            xw[80 + e] = __uint_as_float(r2b[e]);
           }
         }
       }
@@ -1491,13 +1504,19 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       epi_bar_set(set);  // A
       if (!(vote[0] && vote[1] && vote[2] && vote[3])) break;
       const float* xn = xs + ((q + 1) & 3) * 96;  // next quarter (q = 3: rows >= 126 only)
-#pragma unroll 1
-      for (int c0 = 0; c0 < kDxfNt; c0 += 16) {
-        uint32_t r0[16], r1[16], r2[16];
-        ptx::tmem_ld16_nowait(ta + c0, r0);
-        ptx::tmem_ld16_nowait(ta + kDxfNt + c0, r1);
-        ptx::tmem_ld16_nowait(ta + 2 * kDxfNt + c0, r2);
-        ptx::tmem_wait_ld();
+      // all six loads of the tile in flight before one wait
+      uint32_t rr[2][3][16];
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) ptx::tmem_ld16_nowait(ta + dx * kDxfNt + 16 * hh, rr[hh][dx]);
+      ptx::tmem_wait_ld();
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int c0 = 16 * hh;
+        const uint32_t(&r0)[16] = rr[hh][0];
+        const uint32_t(&r1)[16] = rr[hh][1];
+        const uint32_t(&r2)[16] = rr[hh][2];
         float nb1[16], nb2a[16], nb2b[16], bi[16];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
