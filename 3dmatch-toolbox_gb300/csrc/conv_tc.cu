@@ -1454,6 +1454,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
     const int q = warp & 3;
     const int L = q * 32 + lane;  // TMEM lane = row within the CTA's 128 rows
     const int n0 = set * kDxfNt;  // first output channel of this set
+    float bias[kDxfNt];            // this set's 32 biases, kept in registers
+#pragma unroll
+    for (int k = 0; k < kDxfNt / 4; ++k) {
+      const float4 c = __ldg(reinterpret_cast<const float4*>(p.bias + n0) + k);
+      bias[4 * k] = c.x; bias[4 * k + 1] = c.y; bias[4 * k + 2] = c.z; bias[4 * k + 3] = c.w;
+    }
     bool issued = false;
     uint32_t j = 0;
     for (int64_t t = pair; t < p.total_tiles; t += npairs) {
@@ -1517,18 +1523,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
         const uint32_t(&r0)[16] = rr[hh][0];
         const uint32_t(&r1)[16] = rr[hh][1];
         const uint32_t(&r2)[16] = rr[hh][2];
-        float nb1[16], nb2a[16], nb2b[16], bi[16];
+        float nb1[16], nb2a[16], nb2b[16];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const float4 u = reinterpret_cast<const float4*>(xn + c0)[k];
           const float4 w = reinterpret_cast<const float4*>(xn + 32 + c0)[k];
           const float4 z = reinterpret_cast<const float4*>(xn + 64 + c0)[k];
-          const float4 c = __ldg(reinterpret_cast<const float4*>(p.bias + n0 + c0) + k);
           nb1[4 * k] = u.x; nb1[4 * k + 1] = u.y; nb1[4 * k + 2] = u.z; nb1[4 * k + 3] = u.w;
           nb2a[4 * k] = w.x; nb2a[4 * k + 1] = w.y; nb2a[4 * k + 2] = w.z; nb2a[4 * k + 3] = w.w;
           nb2b[4 * k] = z.x; nb2b[4 * k + 1] = z.y; nb2b[4 * k + 2] = z.z; nb2b[4 * k + 3] = z.w;
-          bi[4 * k] = c.x; bi[4 * k + 1] = c.y; bi[4 * k + 2] = c.z; bi[4 * k + 3] = c.w;
         }
+        const float* bi = bias + c0;
         const bool l31 = lane == 31, l30 = lane == 30;
         float v[16];
 #pragma unroll

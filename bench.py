@@ -465,10 +465,10 @@ def run_ours(args, rank, world, local):
         # burst peak: conv2 runs inside a ~14 ms step at full clocks, not a
         # seconds-long loop under the power cap
         peak = peaks["bf16_tflops"] if prec == "bf16" else None
-        roof = {"kernel": "tc_conv_dxf_kernel<2,false> (conv2, %d patches per launch)" % (2 * k),
+        roof = {"kernel": "tc_conv_dxf2_kernel<bf16,x-pooled> (conv2 on CTA pairs, %d patches per launch)" % (2 * k),
                 "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if peak else None, "peak_source": peak_kind + " bf16 burst",
-                "traffic": profile_traffic("conv2_dxf_bf16"),
+                "traffic": profile_traffic("conv2_pair_bf16"),
                 "ms_per_launch": conv2_ms / conv2_n, "share_of_step": (conv2_ms / args.steps) / ms_step}
     layer_ms = {name: round(v[0] / max(1, v[1]), 4) for name, v in lt.items() if v[1]}
     out = None
