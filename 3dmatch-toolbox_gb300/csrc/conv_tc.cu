@@ -1273,9 +1273,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
 //     remote mbarrier arrives;
 //   warps 2-9 (both CTAs): two epilogue sets, set h draining the 96 columns of
 //     channel half h for the CTA's 128 TMEM lanes (the dx row-shift sum of the
-//     kernel above), then signalling the
-//     leader's accumulator-empty barrier (eight local and eight remote
-//     arrivals).
+//     kernel above); each warp signals the leader's accumulator-empty barrier
+//     (eight local and eight remote arrivals) as soon as its accumulator reads
+//     are done, before its arithmetic and stores.
 // TMEM: one pair allocation (issued together by warp 1 of both CTAs), two
 // accumulator buffers of 192 columns.  Every mbarrier wait is bounded; both
 // CTAs always reach the cluster barriers (no early exit), so a timeout in one
@@ -1517,6 +1517,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
 #pragma unroll
         for (int dx = 0; dx < 3; ++dx) ptx::tmem_ld16_nowait(ta + dx * kDxfNt + 16 * hh, rr[hh][dx]);
       ptx::tmem_wait_ld();
+      // this warp has read all it needs of the buffer: hand it back to the MMA
+      // issuer now, before the arithmetic and the stores
+      ptx::tc_fence_before();
+      if (lane == 0) {
+        if (rank == 0) mbar_arrive(accEmpty + 8 * buf);
+        else ptx::mbar_arrive_remote(accEmpty + 8 * buf, 0);
+      }
 #pragma unroll
       for (int hh = 0; hh < 2; ++hh) {
         const int c0 = 16 * hh;
@@ -1582,13 +1589,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
           }
         }
       }
-      ptx::tc_fence_before();
       ptx::fence_proxy_async_smem();  // staging writes visible to the bulk copies
       epi_bar_set(set);               // B
-      if (lane == 0) {
-        if (rank == 0) mbar_arrive(accEmpty + 8 * buf);
-        else ptx::mbar_arrive_remote(accEmpty + 8 * buf, 0);
-      }
       // output runs of this CTA's 126 rows: lane k of quarter 0 takes the k-th
       // grid row (b, z, y) they touch, for this set's chunks
       if (q == 0) {
