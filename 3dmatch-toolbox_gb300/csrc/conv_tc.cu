@@ -143,8 +143,14 @@ __device__ __forceinline__ bool tile_has_work(const KParams& p, int64_t m0, int 
   if (m0 >= p.rows) return false;
   if (p.nyx == 1) return true;
   const int64_t D2 = (int64_t)p.D * p.D, D3 = D2 * p.D;
-  const int64_t r0 = m0 % D3;
+  // 32-bit remainder when the row index fits (every tile loop calls this)
+  const int64_t r0 = p.rows <= INT32_MAX ? (int64_t)((uint32_t)m0 % (uint32_t)D3) : m0 % D3;
   return !(r0 >= (int64_t)p.Do * D2 && r0 + mcta <= D3);
+}
+
+// a / d for row indices: 32-bit unsigned division when the layer's rows fit
+__device__ __forceinline__ int64_t row_div(int64_t a, int d, bool rows32) {
+  return rows32 ? (int64_t)((uint32_t)a / (uint32_t)d) : a / d;
 }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
@@ -812,6 +818,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
     int q0 = 0, np = 0;
     bool ok = true;
     const int64_t plane = (int64_t)p.D * p.D;
+    const bool rows32 = p.rows <= INT32_MAX;
 #ifdef TDM_WAIT_STATS
     const long long t_loop0 = clock64();
 #endif
@@ -830,9 +837,9 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
         base[i] = 0;
         bytes[i] = 0;  // rows past the end are zero-filled
         if (row < p.rows && (i < MSUB || gt < 8)) {
-          const int64_t yz = row / Dx;  // (b, z, y)
+          const int64_t yz = row_div(row, Dx, rows32);  // (b, z, y)
           const int x = (int)(row - yz * Dx);
-          const int64_t b = yz / Do2;
+          const int64_t b = row_div(yz, Do2, rows32);
           const int r = (int)(yz - b * Do2);
           base[i] = ((b * p.D + r / p.Do) * p.D + r % p.Do) * p.D + x;
           bytes[i] = 16;
@@ -1210,13 +1217,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
       if (q < MSUB) {
         const int64_t s0 = m0 + (int64_t)q * kDxfSub;
         const int64_t e0 = min(s0 + kDxfSub, p.rows);
-        const int64_t y0 = s0 / p.D;
+        const bool rows32 = p.rows <= INT32_MAX;
+        const int64_t y0 = row_div(s0, p.D, rows32);
         const int64_t yr = y0 + lane;  // grid row index (b*D + z)*D + y
         const int64_t ra = max(s0, yr * p.D), rb = min(e0, yr * p.D + p.Do);
         if (lane < 6 && ra < rb) {
-          const int64_t bz = yr / p.D;  // b*D + z
+          const int64_t bz = row_div(yr, p.D, rows32);  // b*D + z
           const int y = (int)(yr - bz * p.D);
-          const int64_t b = bz / p.D;
+          const int64_t b = row_div(bz, p.D, rows32);
           const int z = (int)(bz - b * p.D);
           if (y < p.Do && z < p.Do) {
             const int x = (int)(ra - yr * p.D);
@@ -1461,6 +1469,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       bias[4 * k] = c.x; bias[4 * k + 1] = c.y; bias[4 * k + 2] = c.z; bias[4 * k + 3] = c.w;
     }
     bool issued = false;
+    const bool rows32 = p.rows <= INT32_MAX;
     uint32_t j = 0;
     for (int64_t t = pair; t < p.total_tiles; t += npairs) {
       const int64_t m0 = t * kD2Out;
@@ -1489,20 +1498,20 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
         ptx::tmem_ld16_nowait(ta + kDxfNt + 16, r1b);
         ptx::tmem_ld16_nowait(ta + 2 * kDxfNt + 16, r2b);
         ptx::tmem_wait_ld();
-        float* xw = xs + q * 96;
+        uint4* xw = reinterpret_cast<uint4*>(xs + q * 96);
         if (lane == 0) {
 #pragma unroll
-          for (int e = 0; e < 16; ++e) {
-            xw[e] = __uint_as_float(r1a[e]);
-            xw[16 + e] = __uint_as_float(r1b[e]);
-            xw[32 + e] = __uint_as_float(r2a[e]);
-            xw[48 + e] = __uint_as_float(r2b[e]);
+          for (int k = 0; k < 4; ++k) {
+            xw[k] = make_uint4(r1a[4 * k], r1a[4 * k + 1], r1a[4 * k + 2], r1a[4 * k + 3]);
+            xw[4 + k] = make_uint4(r1b[4 * k], r1b[4 * k + 1], r1b[4 * k + 2], r1b[4 * k + 3]);
+            xw[8 + k] = make_uint4(r2a[4 * k], r2a[4 * k + 1], r2a[4 * k + 2], r2a[4 * k + 3]);
+            xw[12 + k] = make_uint4(r2b[4 * k], r2b[4 * k + 1], r2b[4 * k + 2], r2b[4 * k + 3]);
           }
         } else if (lane == 1) {
 #pragma unroll
-          for (int e = 0; e < 16; ++e) {
-            xw[64 + e] = __uint_as_float(r2a[e]);
-            xw[80 + e] = __uint_as_float(r2b[e]);
+          for (int k = 0; k < 4; ++k) {
+            xw[16 + k] = make_uint4(r2a[4 * k], r2a[4 * k + 1], r2a[4 * k + 2], r2a[4 * k + 3]);
+            xw[20 + k] = make_uint4(r2b[4 * k], r2b[4 * k + 1], r2b[4 * k + 2], r2b[4 * k + 3]);
           }
         }
       }
@@ -1596,13 +1605,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       if (q == 0) {
         const int64_t s0 = m0 + (int64_t)rank * kDxfSub;
         const int64_t e0 = min(s0 + kDxfSub, p.rows);
-        const int64_t y0 = s0 / p.D;
+        const int64_t y0 = row_div(s0, p.D, rows32);
         const int64_t yr = y0 + lane;  // grid row index (b*D + z)*D + y
         const int64_t ra = max(s0, yr * p.D), rb = min(e0, yr * p.D + p.Do);
         if (lane < 6 && ra < rb) {
-          const int64_t bz = yr / p.D;
+          const int64_t bz = row_div(yr, p.D, rows32);
           const int y = (int)(yr - bz * p.D);
-          const int64_t b = bz / p.D;
+          const int64_t b = row_div(bz, p.D, rows32);
           const int z = (int)(bz - b * p.D);
           if (y < p.Do && z < p.Do) {
             const int x = (int)(ra - yr * p.D);

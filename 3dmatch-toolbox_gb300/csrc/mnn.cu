@@ -275,6 +275,58 @@ __global__ void rescore_kernel(const float* __restrict__ a, const float* __restr
   if (!skip && (t & 3) == 0) *Q.out = bj;
 }
 
+// Re-scoring of the BF16 form, one warp per query: lane l takes dims
+// [l*dim/32, (l+1)*dim/32) of the query and of its four candidates (coalesced
+// reads), sums (a_k - b_k)^2 in double over its slice, and a shuffle tree adds
+// the 32 slices; the minimum (ties -> lower index) wins.  The sums differ from
+// the oracle's k-ordered ones only in the last bits of double, far below the
+// BF16 candidates' own error; the FP32 form keeps rescore_kernel.
+__global__ void __launch_bounds__(256) rescore_warp_kernel(const float* __restrict__ a, const float* __restrict__ b,
+                                                           int na, int nb, int dim, const int32_t* __restrict__ cand,
+                                                           int32_t* __restrict__ nn_ab, int32_t* __restrict__ nn_ba) {
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (g >= na + nb) return;
+  const Query Q = query_of(g, a, b, na, nb, dim, nn_ab, nn_ba);
+  if (cand[TOPK * g] == -1) return;
+  const int per = dim >> 5, k0 = lane * per;  // dim is a multiple of 64: per is even
+  double part[TOPK];
+  int cj[TOPK];
+#pragma unroll
+  for (int c = 0; c < TOPK; ++c) {
+    const int j = cand[TOPK * g + c];
+    cj[c] = (j >= 0 && j < Q.nr) ? j : -1;
+    part[c] = 0.0;
+  }
+  for (int k = k0; k < k0 + per; k += 2) {
+    const float2 x = *reinterpret_cast<const float2*>(Q.q + k);
+#pragma unroll
+    for (int c = 0; c < TOPK; ++c) {
+      if (cj[c] < 0) continue;
+      const float2 y = *reinterpret_cast<const float2*>(Q.r + (int64_t)cj[c] * dim + k);
+      double d = f2d(x.x) - f2d(y.x);
+      part[c] = fma(d, d, part[c]);
+      d = f2d(x.y) - f2d(y.y);
+      part[c] = fma(d, d, part[c]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < TOPK; ++c)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part[c] += __shfl_xor_sync(0xffffffffu, part[c], o);
+  if (lane == 0) {
+    double best = DBL_MAX;
+    int bj = INT_MAX;
+#pragma unroll
+    for (int c = 0; c < TOPK; ++c)
+      if (cj[c] >= 0 && (part[c] < best || (part[c] == best && cj[c] < bj))) {
+        best = part[c];
+        bj = cj[c];
+      }
+    if (bj != INT_MAX) *Q.out = bj;
+  }
+}
+
 // Full FP64 scan of the listed queries, one block per query at a time.
 __global__ void full_scan_kernel(const float* __restrict__ a, const float* __restrict__ b, int na, int nb, int dim,
                                  const int32_t* __restrict__ full, const int32_t* __restrict__ n_full,
@@ -463,9 +515,13 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
   nn_cols_kernel<<<(nb + 31) / 32, COL_WARPS * 32, 0, s>>>(dot, L.nbp, nb, na, bn, an, maxes, dim, exact, na, cand,
                                                           full, n_full);
   const int64_t lanes = (int64_t)(na + nb) * TOPK;
-  // one warp per block: the FP64 work of 8 queries per warp spreads over every
-  // SM's FP64 pipe instead of packing four warps onto a quarter of the SMs
-  rescore_kernel<<<(unsigned)((lanes + 31) / 32), 32, 0, s>>>(da, db, na, nb, dim, cand, nn_ab, nn_ba);
+  if (exact) {
+    // one warp per block: the FP64 work of 8 queries per warp spreads over every
+    // SM's FP64 pipe instead of packing four warps onto a quarter of the SMs
+    rescore_kernel<<<(unsigned)((lanes + 31) / 32), 32, 0, s>>>(da, db, na, nb, dim, cand, nn_ab, nn_ba);
+  } else {
+    rescore_warp_kernel<<<(unsigned)((na + nb + 7) / 8), 256, 0, s>>>(da, db, na, nb, dim, cand, nn_ab, nn_ba);
+  }
   note_launches(2);
   if (exact) {
     full_scan_kernel<<<256, 256, 0, s>>>(da, db, na, nb, dim, full, n_full, nn_ab, nn_ba);
