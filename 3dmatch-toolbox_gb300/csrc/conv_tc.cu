@@ -1282,8 +1282,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
 //   warps 2-9 (both CTAs): two epilogue sets, set h draining the 96 columns of
 //     channel half h for the CTA's 128 TMEM lanes (the dx row-shift sum of the
 //     kernel above); each warp signals the leader's accumulator-empty barrier
-//     (eight local and eight remote arrivals) as soon as its accumulator reads
-//     are done, before its arithmetic and stores.
+//     (eight local and eight remote arrivals, the remote ones relaxed: a
+//     release at cluster scope held the warp ~1,000 cycles) as soon as its
+//     accumulator reads are done, then adds, packs, takes the x-pair max and
+//     stores each lane's 16-byte chunks straight to global memory (a warp's
+//     even lanes write consecutive pooled rows).  Staging the tile in shared
+//     memory for bulk stores cost the warp issuing them ~2,500 cycles a tile
+//     (two dozen small copies behind the slab loads in the copy engine) and a
+//     second barrier.
 // TMEM: one pair allocation (issued together by warp 1 of both CTAs), two
 // accumulator buffers of 192 columns.  Every mbarrier wait is bounded; both
 // CTAs always reach the cluster barriers (no early exit), so a timeout in one
@@ -1292,11 +1298,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
 // same bits.
 // ---------------------------------------------------------------------------
 constexpr int kD2Threads = 320;
-constexpr int kD2NSA = 3;                 // A slab stages per CTA
+constexpr int kD2NSA = 4;                 // A slab stages per CTA (three per tile: one tile and a third in flight)
 constexpr int kD2N = 2 * kDxfN;           // 192 accumulator columns per buffer
 constexpr int kD2Out = 2 * kDxfSub;       // 252 output rows per pair tile
 constexpr uint32_t kD2Xchg = 2u * 2u * 4u * 96u * 4u;  // [set][parity][quarter][P1 l0, P2 l0, P2 l1] x 32
-constexpr uint32_t kD2Stage = 8u * 128u * 16u;         // output staging [chunk][row][16 B]
 constexpr int kD2Bars = 3 * kD2NSA + 7;
 
 __device__ __forceinline__ void epi_bar_set(int set) {
@@ -1313,8 +1318,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
   uint8_t* sW = smem;
   uint8_t* sA = smem + kDxfWBytes;
   float* sX = reinterpret_cast<float*>(sA + kD2NSA * a_stage);
-  uint8_t* sO = reinterpret_cast<uint8_t*>(sX) + kD2Xchg;
-  int* sVote = reinterpret_cast<int*>(sO + kD2Stage);  // [set][parity][quarter]
+  float* sBias = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(sX) + kD2Xchg);  // the layer's 64 biases
+  int* sVote = reinterpret_cast<int*>(sBias + 64);  // [set][parity][quarter]
   uint64_t* bars = reinterpret_cast<uint64_t*>(sVote + 16);
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + kD2Bars);
 
@@ -1347,6 +1352,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
     ptx::tmem_alloc2(ptx::smem_u32(tmem_holder), TMEM_COLS);
     ptx::tmem_relinquish2();
   }
+  if (threadIdx.x >= 64 && threadIdx.x < 128) sBias[threadIdx.x - 64] = p.bias[threadIdx.x - 64];
   ptx::tc_fence_before();
   __syncthreads();
   ptx::cluster_sync();  // both CTAs' barriers exist before any remote arrive or multicast commit
@@ -1457,112 +1463,113 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
   } else if (!skip) {
     // ---------------- epilogue: set h = channel half h, TMEM lane quarter q = warp % 4 ----------------
     const int set = (warp - 2) >> 2;
-    const uint32_t sO_u = ptx::smem_u32(sO);
-    constexpr int CH = FP8_OUT ? 2 : 4;  // 16-byte output chunks of this set's 32 channels
     const int q = warp & 3;
     const int L = q * 32 + lane;  // TMEM lane = row within the CTA's 128 rows
     const int n0 = set * kDxfNt;  // first output channel of this set
-    float bias[kDxfNt];            // this set's 32 biases, kept in registers
-#pragma unroll
-    for (int k = 0; k < kDxfNt / 4; ++k) {
-      const float4 c = __ldg(reinterpret_cast<const float4*>(p.bias + n0) + k);
-      bias[4 * k] = c.x; bias[4 * k + 1] = c.y; bias[4 * k + 2] = c.z; bias[4 * k + 3] = c.w;
-    }
-    bool issued = false;
     const bool rows32 = p.rows <= INT32_MAX;
+    const int XO = XPOOL ? p.Do / 2 : p.Do;
     uint32_t j = 0;
     for (int64_t t = pair; t < p.total_tiles; t += npairs) {
       const int64_t m0 = t * kD2Out;
       if (!tile_has_work(p, m0, kD2Out)) continue;
       const uint32_t buf = j & 1u, use = j >> 1;
-#ifdef TDM_WAIT_STATS
-      const long long c_w = clock64();
-#endif
+      // this lane's output row s = s0 + L (rows L < 126 of this CTA's half;
+      // x-pooled: the even rows hold the pair maxima) and its output offset
+      int64_t pout = -1;
+      {
+        const int64_t srow = m0 + (int64_t)rank * kDxfSub + L;
+        if (L < kDxfSub && srow < p.rows && (!XPOOL || (L & 1) == 0)) {
+          const int64_t yr = row_div(srow, p.D, rows32);  // (b*D + z)*D + y
+          const int x = (int)(srow - yr * p.D);
+          const int64_t bz = row_div(yr, p.D, rows32);
+          const int y = (int)(yr - bz * p.D);
+          const int64_t b = row_div(bz, p.D, rows32);
+          const int z = (int)(bz - b * p.D);
+          if (x < p.Do && y < p.Do && z < p.Do) pout = ((b * p.Do + z) * p.Do + y) * XO + (XPOOL ? x / 2 : x);
+        }
+      }
       const int got = __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0);
-#ifdef TDM_WAIT_STATS
-      if (lane == 0) atomicAdd(&g_wait_stats[5], (unsigned long long)(clock64() - c_w));
-#endif
       int* vote = sVote + (set * 2 + (j & 1u)) * 4;
       if (lane == 0) vote[q] = got;
-      // exchange: the previous quarter's lanes 30 and 31 need this quarter's
-      // lane 0 (P1, P2) and lane 1 (P2) values (rows +1 and +2 cross the
-      // 32-lane boundary); published before barrier A
+      // The exchange: the previous quarter's lanes 30 and 31 need this
+      // quarter's lane 0 (P1, P2) and lane 1 (P2) values (rows +1 and +2 cross
+      // the 32-lane boundary), published before barrier A.  The buffers
+      // alternate by tile parity: tile j + 2 writes them only after every warp
+      // of the set has passed barrier A of tile j + 1, i.e. finished reading
+      // tile j's.
       float* xs = sX + (set * 2 + (j & 1u)) * (4 * 96);
       const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * kD2N + set * kDxfN;
+      uint32_t rr[2][3][16];
       if (got) {
         ptx::tc_fence_after();
-        // all four loads in flight before one wait
-        uint32_t r1a[16], r2a[16], r1b[16], r2b[16];
-        ptx::tmem_ld16_nowait(ta + kDxfNt, r1a);
-        ptx::tmem_ld16_nowait(ta + 2 * kDxfNt, r2a);
-        ptx::tmem_ld16_nowait(ta + kDxfNt + 16, r1b);
-        ptx::tmem_ld16_nowait(ta + 2 * kDxfNt + 16, r2b);
+        // all six loads of the tile in flight before one wait
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx) ptx::tmem_ld16_nowait(ta + dx * kDxfNt + 16 * hh, rr[hh][dx]);
         ptx::tmem_wait_ld();
+        // this warp has read all it needs of the buffer: hand it back to the
+        // MMA issuer now, before the exchange, the arithmetic and the stores
+        ptx::tc_fence_before();
+        if (lane == 0) {
+          if (rank == 0) mbar_arrive(accEmpty + 8 * buf);
+          else ptx::mbar_arrive_remote_relaxed(accEmpty + 8 * buf, 0);
+        }
         uint4* xw = reinterpret_cast<uint4*>(xs + q * 96);
         if (lane == 0) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            xw[k] = make_uint4(r1a[4 * k], r1a[4 * k + 1], r1a[4 * k + 2], r1a[4 * k + 3]);
-            xw[4 + k] = make_uint4(r1b[4 * k], r1b[4 * k + 1], r1b[4 * k + 2], r1b[4 * k + 3]);
-            xw[8 + k] = make_uint4(r2a[4 * k], r2a[4 * k + 1], r2a[4 * k + 2], r2a[4 * k + 3]);
-            xw[12 + k] = make_uint4(r2b[4 * k], r2b[4 * k + 1], r2b[4 * k + 2], r2b[4 * k + 3]);
-          }
+          for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const uint32_t(&r1)[16] = rr[hh][1];
+              const uint32_t(&r2)[16] = rr[hh][2];
+              xw[4 * hh + k] = make_uint4(r1[4 * k], r1[4 * k + 1], r1[4 * k + 2], r1[4 * k + 3]);
+              xw[8 + 4 * hh + k] = make_uint4(r2[4 * k], r2[4 * k + 1], r2[4 * k + 2], r2[4 * k + 3]);
+            }
         } else if (lane == 1) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            xw[16 + k] = make_uint4(r2a[4 * k], r2a[4 * k + 1], r2a[4 * k + 2], r2a[4 * k + 3]);
-            xw[20 + k] = make_uint4(r2b[4 * k], r2b[4 * k + 1], r2b[4 * k + 2], r2b[4 * k + 3]);
-          }
+          for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const uint32_t(&r2)[16] = rr[hh][2];
+              xw[16 + 4 * hh + k] = make_uint4(r2[4 * k], r2[4 * k + 1], r2[4 * k + 2], r2[4 * k + 3]);
+            }
         }
       }
-      if (issued) ptx::bulk_wait_read_all();  // the staging area is free again
       epi_bar_set(set);  // A
       if (!(vote[0] && vote[1] && vote[2] && vote[3])) break;
       const float* xn = xs + ((q + 1) & 3) * 96;  // next quarter (q = 3: rows >= 126 only)
-      // all six loads of the tile in flight before one wait
-      uint32_t rr[2][3][16];
-#pragma unroll
-      for (int hh = 0; hh < 2; ++hh)
-#pragma unroll
-        for (int dx = 0; dx < 3; ++dx) ptx::tmem_ld16_nowait(ta + dx * kDxfNt + 16 * hh, rr[hh][dx]);
-      ptx::tmem_wait_ld();
-      // this warp has read all it needs of the buffer: hand it back to the MMA
-      // issuer now, before the arithmetic and the stores
-      ptx::tc_fence_before();
-      if (lane == 0) {
-        if (rank == 0) mbar_arrive(accEmpty + 8 * buf);
-        else ptx::mbar_arrive_remote(accEmpty + 8 * buf, 0);
-      }
 #pragma unroll
       for (int hh = 0; hh < 2; ++hh) {
         const int c0 = 16 * hh;
         const uint32_t(&r0)[16] = rr[hh][0];
         const uint32_t(&r1)[16] = rr[hh][1];
         const uint32_t(&r2)[16] = rr[hh][2];
-        float nb1[16], nb2a[16], nb2b[16];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const float4 u = reinterpret_cast<const float4*>(xn + c0)[k];
-          const float4 w = reinterpret_cast<const float4*>(xn + 32 + c0)[k];
-          const float4 z = reinterpret_cast<const float4*>(xn + 64 + c0)[k];
-          nb1[4 * k] = u.x; nb1[4 * k + 1] = u.y; nb1[4 * k + 2] = u.z; nb1[4 * k + 3] = u.w;
-          nb2a[4 * k] = w.x; nb2a[4 * k + 1] = w.y; nb2a[4 * k + 2] = w.z; nb2a[4 * k + 3] = w.w;
-          nb2b[4 * k] = z.x; nb2b[4 * k + 1] = z.y; nb2b[4 * k + 2] = z.z; nb2b[4 * k + 3] = z.w;
-        }
-        const float* bi = bias + c0;
         const bool l31 = lane == 31, l30 = lane == 30;
         float v[16];
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          float s1 = __shfl_down_sync(0xffffffffu, __uint_as_float(r1[e]), 1);
-          float s2 = __shfl_down_sync(0xffffffffu, __uint_as_float(r2[e]), 2);
-          s1 = l31 ? nb1[e] : s1;
-          s2 = l31 ? nb2b[e] : (l30 ? nb2a[e] : s2);
-          const float a = ((__uint_as_float(r0[e]) + s1) + s2) + bi[e];
-          v[e] = p.relu ? fmaxf(a, 0.0f) : a;
+        for (int k = 0; k < 4; ++k) {
+          // neighbour-quarter values and biases: broadcast shared-memory loads,
+          // four channels at a time
+          const float4 u = reinterpret_cast<const float4*>(xn + c0)[k];
+          const float4 w = reinterpret_cast<const float4*>(xn + 32 + c0)[k];
+          const float4 z = reinterpret_cast<const float4*>(xn + 64 + c0)[k];
+          const float4 c = reinterpret_cast<const float4*>(sBias + n0 + c0)[k];
+          const float nb1[4] = {u.x, u.y, u.z, u.w}, nb2a[4] = {w.x, w.y, w.z, w.w};
+          const float nb2b[4] = {z.x, z.y, z.z, z.w}, bi[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int e = 4 * k + i;
+            float s1 = __shfl_down_sync(0xffffffffu, __uint_as_float(r1[e]), 1);
+            float s2 = __shfl_down_sync(0xffffffffu, __uint_as_float(r2[e]), 2);
+            s1 = l31 ? nb1[i] : s1;
+            s2 = l31 ? nb2b[i] : (l30 ? nb2a[i] : s2);
+            const float a = ((__uint_as_float(r0[e]) + s1) + s2) + bi[i];
+            v[e] = p.relu ? fmaxf(a, 0.0f) : a;
+          }
         }
-        const bool stage = !XPOOL || (L & 1) == 0;
-        const int SL = XPOOL ? (L >> 1) : L;
+        // stores straight from registers: chunk-planar output, 16 B per row
+        // and chunk; a warp's even lanes write consecutive pooled rows
         if (FP8_OUT) {
           uint4 o;
           o.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
@@ -1575,7 +1582,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
             o.z = __vmaxu4(o.z, __shfl_xor_sync(0xffffffffu, o.z, 1));
             o.w = __vmaxu4(o.w, __shfl_xor_sync(0xffffffffu, o.w, 1));
           }
-          if (stage) *reinterpret_cast<uint4*>(sO + ((set * CH + c0 / 16) * 128 + SL) * 16) = o;
+          if (pout >= 0) *reinterpret_cast<uint4*>(p.out + (int64_t)(n0 / 16 + c0 / 16) * p.out_cs + pout * 16) = o;
         } else {
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
@@ -1594,43 +1601,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
                 w[k] = *reinterpret_cast<uint32_t*>(&m);
               }
             }
-            if (stage) *reinterpret_cast<uint4*>(sO + ((set * CH + c0 / 8 + h) * 128 + SL) * 16) = o;
-          }
-        }
-      }
-      ptx::fence_proxy_async_smem();  // staging writes visible to the bulk copies
-      epi_bar_set(set);               // B
-      // output runs of this CTA's 126 rows: lane k of quarter 0 takes the k-th
-      // grid row (b, z, y) they touch, for this set's chunks
-      if (q == 0) {
-        const int64_t s0 = m0 + (int64_t)rank * kDxfSub;
-        const int64_t e0 = min(s0 + kDxfSub, p.rows);
-        const int64_t y0 = row_div(s0, p.D, rows32);
-        const int64_t yr = y0 + lane;  // grid row index (b*D + z)*D + y
-        const int64_t ra = max(s0, yr * p.D), rb = min(e0, yr * p.D + p.Do);
-        if (lane < 6 && ra < rb) {
-          const int64_t bz = row_div(yr, p.D, rows32);
-          const int y = (int)(yr - bz * p.D);
-          const int64_t b = row_div(bz, p.D, rows32);
-          const int z = (int)(bz - b * p.D);
-          if (y < p.Do && z < p.Do) {
-            const int x = (int)(ra - yr * p.D);
-            const int XO = XPOOL ? p.Do / 2 : p.Do;
-            const int64_t pout = ((b * p.Do + z) * p.Do + y) * XO + (XPOOL ? x / 2 : x);
-            const uint32_t len = (uint32_t)((rb - ra) / (XPOOL ? 2 : 1)) * 16u;
-            const int srow = (int)(ra - s0) / (XPOOL ? 2 : 1);
-#pragma unroll
-            for (int c = 0; c < CH; ++c)
-              ptx::bulk_s2g(p.out + (int64_t)(n0 / (FP8_OUT ? 16 : 8) + c) * p.out_cs + pout * 16,
-                            sO_u + ((set * CH + c) * 128 + srow) * 16, len);
-            ptx::bulk_commit();
-            issued = true;
+            if (pout >= 0)
+              *reinterpret_cast<uint4*>(p.out + (int64_t)(n0 / 8 + c0 / 8 + h) * p.out_cs + pout * 16) = o;
           }
         }
       }
       ++j;
     }
-    if (issued) ptx::bulk_wait_all();
   }
   ptx::tc_fence_before();
   __syncthreads();
@@ -1887,7 +1864,7 @@ int weight_stages(const TcLayer& L) {
 
 size_t smem_bytes(const TcLayer& L) {
   if (L.dxf && L.pair)
-    return kDxfWBytes + (size_t)kD2NSA * 16 * 8 * pair_slab_rows(L) + kD2Xchg + kD2Stage + 64 + kSmemReserve;
+    return kDxfWBytes + (size_t)kD2NSA * 16 * 8 * pair_slab_rows(L) + kD2Xchg + 256 + 64 + kSmemReserve;
   if (L.dxf) return kDxfWBytes + kDxfNSA * a_stage_bytes(L) + kDxfXchg + kDxfStage + 32 + kSmemReserve;
   if (L.gather)
     return gather_stages(L) * gather_stage_bytes(L) + (L.wt ? kWtStage : 0) + (size_t)weight_stages(L) * L.nt * 128 +
