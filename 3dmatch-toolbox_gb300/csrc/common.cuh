@@ -245,6 +245,25 @@ __device__ __forceinline__ void mbar_arrive_remote_relaxed(uint32_t bar, uint32_
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(bar), "r"(rank));
   asm volatile("mbarrier.arrive.relaxed.cluster.shared::cluster.b64 _, [%0];" ::"r"(remote) : "memory");
 }
+// The shared::cluster address of the same shared-memory offset in CTA `rank`
+// of this cluster.
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank) {
+  uint32_t remote;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(addr), "r"(rank));
+  return remote;
+}
+// Tiled 3-D tensor copy global -> this CTA's shared memory for a CTA pair:
+// the completion (complete_tx) goes to `bar`, a shared::cluster barrier address
+// that may lie in either CTA of the pair.  The innermost coordinate c0 is 0 in
+// every caller (16-byte aligned).
+__device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const void* map, int c0, int c1, int c2,
+                                                 uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+      "%4}], [%5];" ::"r"(dst),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      : "memory");
+}
 // TMEM of a CTA pair: issued by one warp in each of the two CTAs together
 // (the allocation is one, at the same address in both).
 __device__ __forceinline__ void tmem_alloc2(uint32_t dst_smem, uint32_t ncols) {

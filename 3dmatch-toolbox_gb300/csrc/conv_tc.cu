@@ -29,6 +29,7 @@
 //                  other buffer while the next tile accumulates
 // Every wait is bounded; a wait that runs out raises the device error word and
 // the CTA drains its in-flight copies, frees TMEM and exits.
+#include <cuda.h>
 #include <cuda_fp8.h>
 
 #include <algorithm>
@@ -1302,7 +1303,8 @@ constexpr int kD2NSA = 4;                 // A slab stages per CTA (three per ti
 constexpr int kD2N = 2 * kDxfN;           // 192 accumulator columns per buffer
 constexpr int kD2Out = 2 * kDxfSub;       // 252 output rows per pair tile
 constexpr uint32_t kD2Xchg = 2u * 2u * 4u * 96u * 4u;  // [set][parity][quarter][P1 l0, P2 l0, P2 l1] x 32
-constexpr int kD2Bars = 3 * kD2NSA + 7;
+constexpr int kD2Bars = 2 * kD2NSA + 7;
+constexpr int64_t kPairMaxRows = INT32_MAX - (1 << 16);  // slab rows stay below 2^31
 
 __device__ __forceinline__ void epi_bar_set(int set) {
   if (set == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
@@ -1310,7 +1312,8 @@ __device__ __forceinline__ void epi_bar_set(int set) {
 }
 
 template <bool FP8_OUT, bool XPOOL>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_conv_dxf2_kernel(const KParams p) {
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_conv_dxf2_kernel(const KParams p,
+                                                                                          const __grid_constant__ CUtensorMap tmA) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t TMEM_COLS = 512;
   const int R = p.R;
@@ -1329,14 +1332,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
   // meets its peer at both cluster barriers
   const bool skip = !__syncthreads_and(aborted(p.err) ? 0 : 1);
 
-  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * kD2NSA, peerA = emptyA + 8 * kD2NSA;
-  const uint32_t wfull = peerA + 8 * kD2NSA, peerW = wfull + 8, accFull = peerW + 8, accEmpty = accFull + 16,
+  // fullA is used in the leader only (both CTAs' slab copies complete on it)
+  const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * kD2NSA;
+  const uint32_t wfull = emptyA + 8 * kD2NSA, peerW = wfull + 8, accFull = peerW + 8, accEmpty = accFull + 16,
                  done = accEmpty + 16;
   if (threadIdx.x == 0) {
     for (int i = 0; i < kD2NSA; ++i) {
       ptx::mbar_init(fullA + 8 * i, 1);
       ptx::mbar_init(emptyA + 8 * i, 1);
-      ptx::mbar_init(peerA + 8 * i, 1);
     }
     ptx::mbar_init(wfull, 1);
     ptx::mbar_init(peerW, 1);
@@ -1369,6 +1372,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       for (int b = 0; b < 9; ++b)
         ptx::bulk_g2s(sW_u + b * kDxfBlock, p.wpk + (size_t)rank * kDxfWBytes + (size_t)b * kDxfBlock, kDxfBlock,
                       wfull);
+      // Slabs: one tiled copy of [8 chunks][R rows][16 B] per stage.  Both
+      // CTAs' copies complete on the leader's fullA (the leader expects both
+      // halves' bytes), so the MMA issuer waits on one local barrier per stage.
+      // The peer loads stage s of use k only after the MMAs of use k - 1 freed
+      // it (emptyA, multicast), i.e. after the leader's fullA left that phase.
+      const uint32_t fullA_lead = ptx::mapa_shared(fullA, 0);
       int sa = 0;
       uint32_t pha = 0;
       int armedA[kD2NSA];
@@ -1380,34 +1389,28 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
         const int64_t s0 = m0 + (int64_t)rank * kDxfSub;
         for (int zt = 0; zt < 3; ++zt) {
           if (!TDM_TIMED_WAIT(3, wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
-          ptx::mbar_arrive_expect_tx(fullA + 8 * sa, a_stage);
+          if (rank == 0) ptx::mbar_arrive_expect_tx(fullA + 8 * sa, 2 * a_stage);
           armedA[sa] = (int)pha;
-          const uint8_t* src = p.act + (s0 + zt * plane) * 16;
-          for (int j = 0; j < 8; ++j)
-            ptx::bulk_g2s(sA_u + sa * a_stage + j * R * 16, src + j * p.act_cs, R * 16, fullA + 8 * sa);
+          ptx::tma_load_3d_pair(sA_u + sa * a_stage, &tmA, 0, (int)(s0 + zt * plane), 0, fullA_lead + 8 * sa);
           if (++sa == kD2NSA) { sa = 0; pha ^= 1; }
         }
       }
-      for (int i = 0; i < kD2NSA; ++i)
-        if (armedA[i] >= 0) wait_or_flag(fullA + 8 * i, (uint32_t)armedA[i], p.err, DEV_TIMEOUT_PRODUCER);
+      if (rank == 0) {
+        // the leader's fullA phases cover both CTAs' copies
+        for (int i = 0; i < kD2NSA; ++i)
+          if (armedA[i] >= 0) wait_or_flag(fullA + 8 * i, (uint32_t)armedA[i], p.err, DEV_TIMEOUT_PRODUCER);
+      } else if (aborted(p.err)) {
+        // the peer cannot see its copies complete; after an abort it gives
+        // any still in flight 200 us (one lands within a few microseconds)
+        const uint64_t t0 = ptx::globaltimer_ns();
+        while (ptx::globaltimer_ns() - t0 < 200000ull) __nanosleep(1000);
+      }
       wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_PRODUCER);
     }
   } else if (warp == 1) {
     if (lane == 0 && !skip && rank == 1) {
-      // ---------------- peer: relay its copy completions to the leader ----------------
-      bool ok = wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_PRODUCER);
-      if (ok) ptx::mbar_arrive_remote(peerW, 0);
-      int sa = 0;
-      uint32_t pha = 0;
-      for (int64_t t = pair; t < p.total_tiles && ok; t += npairs) {
-        const int64_t m0 = t * kD2Out;
-        if (!tile_has_work(p, m0, kD2Out)) continue;
-        for (int zt = 0; zt < 3; ++zt) {
-          if (!wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
-          ptx::mbar_arrive_remote(peerA + 8 * sa, 0);
-          if (++sa == kD2NSA) { sa = 0; pha ^= 1; }
-        }
-      }
+      // ---------------- peer: relay its weight copy's completion to the leader ----------------
+      if (wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_PRODUCER)) ptx::mbar_arrive_remote(peerW, 0);
     } else if (lane == 0 && !skip && rank == 0) {
       // ---------------- leader: the pair's MMA issuer ----------------
       constexpr uint32_t idesc = ptx::make_idesc(kD2N, 256, 1, 1);
@@ -1429,8 +1432,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
         const uint32_t dbase = tmem + buf * kD2N;
         uint32_t accumulate = 0;
         for (int zt = 0; zt < 3 && ok; ++zt) {
-          if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA)) ||
-              !TDM_TIMED_WAIT(2, wait_or_flag_cluster(peerA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) {
+          if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) {
             ok = false;
             break;
           }
@@ -1984,14 +1986,53 @@ int dxf2_max_pairs(size_t smem) {
   return n;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// The conv2 input as a 3-D byte tensor [8 chunks][plane rows][16 B], read in
+// boxes of one slab: [8][R][16].  Rows past the plane are zero-filled.
+tdm_status slab_tensor_map(const KParams& kp, CUtensorMap* map) {
+  EncodeTiledFn enc = encode_tiled_fn();
+  if (!enc) return fail(TDM_ERR_DEVICE, "cuTensorMapEncodeTiled unavailable");
+  const cuuint64_t dims[3] = {16, (cuuint64_t)(kp.act_cs / 16), 8};
+  const cuuint64_t strides[2] = {16, (cuuint64_t)kp.act_cs};
+  const cuuint32_t box[3] = {16, (cuuint32_t)kp.R, 8};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<uint8_t*>(kp.act), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(TDM_ERR_DEVICE, "cuTensorMapEncodeTiled failed for the conv2 slab map");
+  return TDM_OK;
+}
+
 template <bool FP8_OUT, bool XPOOL>
 tdm_status launch_dxf2(const KParams& kp, size_t smem, cudaStream_t s) {
   auto kern = tc_conv_dxf2_kernel<FP8_OUT, XPOOL>;
   cudaError_t attr_err = raise_smem_cap(reinterpret_cast<const void*>(kern), (int)kSmemLimit);
   if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_dxf2_kernel)");
+  CUtensorMap map;
+  tdm_status st = slab_tensor_map(kp, &map);
+  if (st) return st;
   // persistent: no more pairs than fit at once, so every pair runs from the start
   const int64_t pairs = std::max<int64_t>(1, std::min<int64_t>(kp.total_tiles, dxf2_max_pairs<FP8_OUT, XPOOL>(smem)));
-  kern<<<(unsigned)(2 * pairs), kD2Threads, smem, s>>>(kp);
+  kern<<<(unsigned)(2 * pairs), kD2Threads, smem, s>>>(kp, map);
   TDM_CHECK_LAUNCH("tc_conv_dxf2_kernel");
   return TDM_OK;
 }
@@ -2101,6 +2142,13 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   kp.R = slab_rows(L);
   kp.err = device_error_word();
   if (!kp.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
+  if (L.dxf && L.pair && a.rows > kPairMaxRows) {
+    // slab rows are 32-bit tensor coordinates: larger inputs take the
+    // single-CTA form (same bits)
+    TcLayer L1 = L;
+    L1.pair = false;
+    return launch_tc_layer(L1, a, s);
+  }
   if (L.dxf && L.pair) {
     TDM_REQUIRE(tc_layer_fits(L), "tc layer: unsupported dx-fused pair tile");
     TDM_REQUIRE((reinterpret_cast<uintptr_t>(a.act) & 15) == 0 && (a.act_cs & 15) == 0 &&
