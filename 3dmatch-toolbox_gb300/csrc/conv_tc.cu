@@ -1391,7 +1391,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
           if (!TDM_TIMED_WAIT(3, wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
           if (rank == 0) ptx::mbar_arrive_expect_tx(fullA + 8 * sa, 2 * a_stage);
           armedA[sa] = (int)pha;
-          ptx::tma_load_3d_pair(sA_u + sa * a_stage, &tmA, 0, (int)(s0 + zt * plane), 0, fullA_lead + 8 * sa);
+          ptx::tma_load_3d_pair(sA_u + sa * a_stage, &tmA, 0, (int)((s0 + zt * plane) >> 1), 0, fullA_lead + 8 * sa);
           if (++sa == kD2NSA) { sa = 0; pha ^= 1; }
         }
       }
@@ -2006,14 +2006,15 @@ EncodeTiledFn encode_tiled_fn() {
   return fn;
 }
 
-// The conv2 input as a 3-D byte tensor [8 chunks][plane rows][16 B], read in
-// boxes of one slab: [8][R][16].  Rows past the plane are zero-filled.
+// The conv2 input as a 3-D byte tensor [8 chunks][plane rows / 2][32 B] (two
+// 16-byte rows per line: every slab starts on an even row), read in boxes of
+// one slab: [8][R / 2][32].  Lines past the plane are zero-filled.
 tdm_status slab_tensor_map(const KParams& kp, CUtensorMap* map) {
   EncodeTiledFn enc = encode_tiled_fn();
   if (!enc) return fail(TDM_ERR_DEVICE, "cuTensorMapEncodeTiled unavailable");
-  const cuuint64_t dims[3] = {16, (cuuint64_t)(kp.act_cs / 16), 8};
-  const cuuint64_t strides[2] = {16, (cuuint64_t)kp.act_cs};
-  const cuuint32_t box[3] = {16, (cuuint32_t)kp.R, 8};
+  const cuuint64_t dims[3] = {32, (cuuint64_t)(kp.act_cs / 32), 8};
+  const cuuint64_t strides[2] = {32, (cuuint64_t)kp.act_cs};
+  const cuuint32_t box[3] = {32, (cuuint32_t)kp.R / 2, 8};
   const cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<uint8_t*>(kp.act), dims, strides, box, estr,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
