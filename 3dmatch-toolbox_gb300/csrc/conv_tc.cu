@@ -1298,22 +1298,33 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
 // The sums are the kernel above's in the same order, so the outputs are the
 // same bits.
 // ---------------------------------------------------------------------------
-constexpr int kD2Threads = 320;
+constexpr int kD2EpiWarps = 16;                      // four sets of 16 channels x four lane quarters
+constexpr int kD2Threads = 32 * (2 + kD2EpiWarps);
 constexpr int kD2NSA = 4;                 // A slab stages per CTA (three per tile: one tile and a third in flight)
 constexpr int kD2N = 2 * kDxfN;           // 192 accumulator columns per buffer
 constexpr int kD2Out = 2 * kDxfSub;       // 252 output rows per pair tile
-constexpr uint32_t kD2Xchg = 2u * 2u * 4u * 96u * 4u;  // [set][parity][quarter][P1 l0, P2 l0, P2 l1] x 32
+constexpr uint32_t kD2Xchg = 4u * 2u * 4u * 48u * 4u;  // [set][parity][quarter][P1 l0, P2 l0, P2 l1] x 16
 constexpr int kD2Bars = 2 * kD2NSA + 7;
 constexpr int64_t kPairMaxRows = INT32_MAX - (1 << 16);  // slab rows stay below 2^31
 
+// Epilogue row bookkeeping of the pair kernel, fixed per launch: the tile
+// step npairs * 252 rows as digits of the input grid (sx, sy, sz, sb) and
+// modulo D^3 (rstep), the first z-tail row zcut = Do * D^2, and the
+// multiply-shift constant ceil(2^20 / D) for x digits below 256.
+struct PairSched {
+  uint32_t rows, step, rstep, D3, zcut, magic;
+  int sx, sy, sz, sb;
+};
+
 __device__ __forceinline__ void epi_bar_set(int set) {
-  if (set == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
-  else asm volatile("bar.sync 2, 128;" ::: "memory");
+  // named barriers 1..4 (0 is __syncthreads), one per epilogue set of 4 warps
+  asm volatile("bar.sync %0, 128;" ::"r"(set + 1) : "memory");
 }
 
 template <bool FP8_OUT, bool XPOOL>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_conv_dxf2_kernel(const KParams p,
-                                                                                          const __grid_constant__ CUtensorMap tmA) {
+                                                                                          const __grid_constant__ CUtensorMap tmA,
+                                                                                          const PairSched ps) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t TMEM_COLS = 512;
   const int R = p.R;
@@ -1323,7 +1334,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
   float* sX = reinterpret_cast<float*>(sA + kD2NSA * a_stage);
   float* sBias = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(sX) + kD2Xchg);  // the layer's 64 biases
   int* sVote = reinterpret_cast<int*>(sBias + 64);  // [set][parity][quarter]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sVote + 16);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sVote + 32);
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + kD2Bars);
 
   const uint32_t rank = ptx::cluster_rank();
@@ -1345,7 +1356,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
     ptx::mbar_init(peerW, 1);
     for (int i = 0; i < 2; ++i) {
       ptx::mbar_init(accFull + 8 * i, 1);
-      ptx::mbar_init(accEmpty + 8 * i, 16);  // 8 epilogue warps here, 8 in the peer
+      ptx::mbar_init(accEmpty + 8 * i, 2 * kD2EpiWarps);  // every epilogue warp of both CTAs
     }
     ptx::mbar_init(done, 1);
     ptx::fence_barrier_init();
@@ -1463,33 +1474,63 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       wait_or_flag(done, 0, p.err, DEV_TIMEOUT_MMA);
     }
   } else if (!skip) {
-    // ---------------- epilogue: set h = channel half h, TMEM lane quarter q = warp % 4 ----------------
-    const int set = (warp - 2) >> 2;
+    // ---------------- epilogue: set = 16 output channels, TMEM lane quarter q = warp % 4 ----------------
+    const int set = (warp - 2) >> 2;  // 0..3
     const int q = warp & 3;
     const int L = q * 32 + lane;  // TMEM lane = row within the CTA's 128 rows
-    const int n0 = set * kDxfNt;  // first output channel of this set
-    const bool rows32 = p.rows <= INT32_MAX;
-    const int XO = XPOOL ? p.Do / 2 : p.Do;
+    const int n0 = set * 16;      // first output channel of this set
+    // this set's columns: channel half set / 2 (the 96 columns of its dx taps),
+    // 16 channels at (set % 2) * 16 within each tap's 32
+    const uint32_t col0 = (uint32_t)((set >> 1) * kDxfN + (set & 1) * 16);
+    // Row bookkeeping in 32 bits without divisions in the loop (the host sends
+    // inputs of 2^31 - 2^16 rows or more, or grids with D < 12, to the
+    // single-CTA form).  Warp-uniform: the first row s0 = m0 + rank * 126 of
+    // this CTA's half as digits (ux, uy, uz, ub) of the input grid and the
+    // tile's first row within its patch r0 = m0 % D^3, advanced by
+    // npairs * 252 rows per tile step.  Per lane: row s0 + L, whose x digit
+    // ux + L < 256 is split by a multiply-shift (exact for n < 2^20 / D).
+    // The loop constants come from the kernel parameters (PairSched), which
+    // instructions read in place without holding registers.
+    const int D = p.D, Do = p.Do, XO = XPOOL ? p.Do / 2 : p.Do;
+    uint32_t m0 = (uint32_t)(pair * kD2Out), r0 = m0 % ps.D3, s0 = m0 + rank * kDxfSub;
+    int ux = (int)(s0 % D), uy = (int)(s0 / D % D), uz = (int)(s0 / (D * D) % D), ub = (int)(s0 / ps.D3);
+    uint8_t* const outp = p.out + (int64_t)(n0 / (FP8_OUT ? 16 : 8)) * p.out_cs;
     uint32_t j = 0;
-    for (int64_t t = pair; t < p.total_tiles; t += npairs) {
-      const int64_t m0 = t * kD2Out;
-      if (!tile_has_work(p, m0, kD2Out)) continue;
-      const uint32_t buf = j & 1u, use = j >> 1;
-      // this lane's output row s = s0 + L (rows L < 126 of this CTA's half;
-      // x-pooled: the even rows hold the pair maxima) and its output offset
-      int64_t pout = -1;
+    for (int t = (int)pair; t < (int)p.total_tiles; t += (int)npairs) {
+      // the same test as tile_has_work, from r0
+      const bool work = m0 < ps.rows && (p.nyx == 1 || !(r0 >= ps.zcut && r0 + kD2Out <= ps.D3));
+      // this lane's output offset (rows L < 126 of this CTA's half; x-pooled:
+      // the even rows hold the pair maxima), or -1
+      int pout = -1;
       {
-        const int64_t srow = m0 + (int64_t)rank * kDxfSub + L;
-        if (L < kDxfSub && srow < p.rows && (!XPOOL || (L & 1) == 0)) {
-          const int64_t yr = row_div(srow, p.D, rows32);  // (b*D + z)*D + y
-          const int x = (int)(srow - yr * p.D);
-          const int64_t bz = row_div(yr, p.D, rows32);
-          const int y = (int)(yr - bz * p.D);
-          const int64_t b = row_div(bz, p.D, rows32);
-          const int z = (int)(bz - b * p.D);
-          if (x < p.Do && y < p.Do && z < p.Do) pout = ((b * p.Do + z) * p.Do + y) * XO + (XPOOL ? x / 2 : x);
-        }
+        const int n = ux + L, cy = (int)(((uint32_t)n * ps.magic) >> 20), x = n - cy * D;
+        int y = uy + cy, c = y >= D;
+        y -= c ? D : 0;
+        int z = uz + c;
+        c = z >= D;
+        z -= c ? D : 0;
+        const int bb = ub + c;
+        if (L < kDxfSub && s0 + L < ps.rows && x < Do && y < Do && z < Do && (!XPOOL || (x & 1) == 0))
+          pout = ((bb * Do + z) * Do + y) * XO + (XPOOL ? x / 2 : x);
       }
+      {  // advance to tile t + npairs
+        m0 += ps.step;
+        s0 += ps.step;
+        r0 += ps.rstep;
+        r0 -= r0 >= ps.D3 ? ps.D3 : 0;
+        ux += ps.sx;
+        int c = ux >= D;
+        ux -= c ? D : 0;
+        uy += ps.sy + c;
+        c = uy >= D;
+        uy -= c ? D : 0;
+        uz += ps.sz + c;
+        c = uz >= D;
+        uz -= c ? D : 0;
+        ub += ps.sb + c;
+      }
+      if (!work) continue;
+      const uint32_t buf = j & 1u, use = j >> 1;
       const int got = __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0);
       int* vote = sVote + (set * 2 + (j & 1u)) * 4;
       if (lane == 0) vote[q] = got;
@@ -1499,16 +1540,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       // alternate by tile parity: tile j + 2 writes them only after every warp
       // of the set has passed barrier A of tile j + 1, i.e. finished reading
       // tile j's.
-      float* xs = sX + (set * 2 + (j & 1u)) * (4 * 96);
-      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * kD2N + set * kDxfN;
-      uint32_t rr[2][3][16];
+      float* xs = sX + (set * 2 + (j & 1u)) * (4 * 48);
+      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * kD2N + col0;
+      uint32_t r0v[16], r1v[16], r2v[16];
       if (got) {
         ptx::tc_fence_after();
-        // all six loads of the tile in flight before one wait
-#pragma unroll
-        for (int hh = 0; hh < 2; ++hh)
-#pragma unroll
-          for (int dx = 0; dx < 3; ++dx) ptx::tmem_ld16_nowait(ta + dx * kDxfNt + 16 * hh, rr[hh][dx]);
+        // all three loads in flight before one wait
+        ptx::tmem_ld16_nowait(ta, r0v);
+        ptx::tmem_ld16_nowait(ta + kDxfNt, r1v);
+        ptx::tmem_ld16_nowait(ta + 2 * kDxfNt, r2v);
         ptx::tmem_wait_ld();
         // this warp has read all it needs of the buffer: hand it back to the
         // MMA issuer now, before the exchange, the arithmetic and the stores
@@ -1517,95 +1557,78 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
           if (rank == 0) mbar_arrive(accEmpty + 8 * buf);
           else ptx::mbar_arrive_remote_relaxed(accEmpty + 8 * buf, 0);
         }
-        uint4* xw = reinterpret_cast<uint4*>(xs + q * 96);
+        uint4* xw = reinterpret_cast<uint4*>(xs + q * 48);
         if (lane == 0) {
 #pragma unroll
-          for (int hh = 0; hh < 2; ++hh)
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const uint32_t(&r1)[16] = rr[hh][1];
-              const uint32_t(&r2)[16] = rr[hh][2];
-              xw[4 * hh + k] = make_uint4(r1[4 * k], r1[4 * k + 1], r1[4 * k + 2], r1[4 * k + 3]);
-              xw[8 + 4 * hh + k] = make_uint4(r2[4 * k], r2[4 * k + 1], r2[4 * k + 2], r2[4 * k + 3]);
-            }
+          for (int k = 0; k < 4; ++k) {
+            xw[k] = make_uint4(r1v[4 * k], r1v[4 * k + 1], r1v[4 * k + 2], r1v[4 * k + 3]);
+            xw[4 + k] = make_uint4(r2v[4 * k], r2v[4 * k + 1], r2v[4 * k + 2], r2v[4 * k + 3]);
+          }
         } else if (lane == 1) {
 #pragma unroll
-          for (int hh = 0; hh < 2; ++hh)
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const uint32_t(&r2)[16] = rr[hh][2];
-              xw[16 + 4 * hh + k] = make_uint4(r2[4 * k], r2[4 * k + 1], r2[4 * k + 2], r2[4 * k + 3]);
-            }
+          for (int k = 0; k < 4; ++k) xw[8 + k] = make_uint4(r2v[4 * k], r2v[4 * k + 1], r2v[4 * k + 2], r2v[4 * k + 3]);
         }
       }
       epi_bar_set(set);  // A
       if (!(vote[0] && vote[1] && vote[2] && vote[3])) break;
-      const float* xn = xs + ((q + 1) & 3) * 96;  // next quarter (q = 3: rows >= 126 only)
+      const float* xn = xs + ((q + 1) & 3) * 48;  // next quarter (q = 3: rows >= 126 only)
+      const bool l31 = lane == 31, l30 = lane == 30;
+      float v[16];
 #pragma unroll
-      for (int hh = 0; hh < 2; ++hh) {
-        const int c0 = 16 * hh;
-        const uint32_t(&r0)[16] = rr[hh][0];
-        const uint32_t(&r1)[16] = rr[hh][1];
-        const uint32_t(&r2)[16] = rr[hh][2];
-        const bool l31 = lane == 31, l30 = lane == 30;
-        float v[16];
+      for (int k = 0; k < 4; ++k) {
+        // neighbour-quarter values and biases: broadcast shared-memory loads,
+        // four channels at a time
+        const float4 u = reinterpret_cast<const float4*>(xn)[k];
+        const float4 w = reinterpret_cast<const float4*>(xn + 16)[k];
+        const float4 zz = reinterpret_cast<const float4*>(xn + 32)[k];
+        const float4 c = reinterpret_cast<const float4*>(sBias + n0)[k];
+        const float nb1[4] = {u.x, u.y, u.z, u.w}, nb2a[4] = {w.x, w.y, w.z, w.w};
+        const float nb2b[4] = {zz.x, zz.y, zz.z, zz.w}, bi[4] = {c.x, c.y, c.z, c.w};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          // neighbour-quarter values and biases: broadcast shared-memory loads,
-          // four channels at a time
-          const float4 u = reinterpret_cast<const float4*>(xn + c0)[k];
-          const float4 w = reinterpret_cast<const float4*>(xn + 32 + c0)[k];
-          const float4 z = reinterpret_cast<const float4*>(xn + 64 + c0)[k];
-          const float4 c = reinterpret_cast<const float4*>(sBias + n0 + c0)[k];
-          const float nb1[4] = {u.x, u.y, u.z, u.w}, nb2a[4] = {w.x, w.y, w.z, w.w};
-          const float nb2b[4] = {z.x, z.y, z.z, z.w}, bi[4] = {c.x, c.y, c.z, c.w};
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const int e = 4 * k + i;
-            float s1 = __shfl_down_sync(0xffffffffu, __uint_as_float(r1[e]), 1);
-            float s2 = __shfl_down_sync(0xffffffffu, __uint_as_float(r2[e]), 2);
-            s1 = l31 ? nb1[i] : s1;
-            s2 = l31 ? nb2b[i] : (l30 ? nb2a[i] : s2);
-            const float a = ((__uint_as_float(r0[e]) + s1) + s2) + bi[i];
-            v[e] = p.relu ? fmaxf(a, 0.0f) : a;
-          }
+        for (int i = 0; i < 4; ++i) {
+          const int e = 4 * k + i;
+          float s1 = __shfl_down_sync(0xffffffffu, __uint_as_float(r1v[e]), 1);
+          float s2 = __shfl_down_sync(0xffffffffu, __uint_as_float(r2v[e]), 2);
+          s1 = l31 ? nb1[i] : s1;
+          s2 = l31 ? nb2b[i] : (l30 ? nb2a[i] : s2);
+          const float a = ((__uint_as_float(r0v[e]) + s1) + s2) + bi[i];
+          v[e] = p.relu ? fmaxf(a, 0.0f) : a;
         }
-        // stores straight from registers: chunk-planar output, 16 B per row
-        // and chunk; a warp's even lanes write consecutive pooled rows
-        if (FP8_OUT) {
+      }
+      // stores straight from registers: chunk-planar output, 16 B per row
+      // and chunk; a warp's even lanes write consecutive pooled rows
+      if (FP8_OUT) {
+        uint4 o;
+        o.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
+        o.y = pack_e4m3x4(v[4] * p.out_qinv, v[5] * p.out_qinv, v[6] * p.out_qinv, v[7] * p.out_qinv);
+        o.z = pack_e4m3x4(v[8] * p.out_qinv, v[9] * p.out_qinv, v[10] * p.out_qinv, v[11] * p.out_qinv);
+        o.w = pack_e4m3x4(v[12] * p.out_qinv, v[13] * p.out_qinv, v[14] * p.out_qinv, v[15] * p.out_qinv);
+        if (XPOOL) {
+          o.x = __vmaxu4(o.x, __shfl_xor_sync(0xffffffffu, o.x, 1));
+          o.y = __vmaxu4(o.y, __shfl_xor_sync(0xffffffffu, o.y, 1));
+          o.z = __vmaxu4(o.z, __shfl_xor_sync(0xffffffffu, o.z, 1));
+          o.w = __vmaxu4(o.w, __shfl_xor_sync(0xffffffffu, o.w, 1));
+        }
+        if (pout >= 0) *reinterpret_cast<uint4*>(outp + (int64_t)pout * 16) = o;
+      } else {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
           uint4 o;
-          o.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
-          o.y = pack_e4m3x4(v[4] * p.out_qinv, v[5] * p.out_qinv, v[6] * p.out_qinv, v[7] * p.out_qinv);
-          o.z = pack_e4m3x4(v[8] * p.out_qinv, v[9] * p.out_qinv, v[10] * p.out_qinv, v[11] * p.out_qinv);
-          o.w = pack_e4m3x4(v[12] * p.out_qinv, v[13] * p.out_qinv, v[14] * p.out_qinv, v[15] * p.out_qinv);
+          o.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
+          o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
+          o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
+          o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
           if (XPOOL) {
-            o.x = __vmaxu4(o.x, __shfl_xor_sync(0xffffffffu, o.x, 1));
-            o.y = __vmaxu4(o.y, __shfl_xor_sync(0xffffffffu, o.y, 1));
-            o.z = __vmaxu4(o.z, __shfl_xor_sync(0xffffffffu, o.z, 1));
-            o.w = __vmaxu4(o.w, __shfl_xor_sync(0xffffffffu, o.w, 1));
-          }
-          if (pout >= 0) *reinterpret_cast<uint4*>(p.out + (int64_t)(n0 / 16 + c0 / 16) * p.out_cs + pout * 16) = o;
-        } else {
+            uint32_t* w = reinterpret_cast<uint32_t*>(&o);
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            uint4 o;
-            o.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
-            o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
-            o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
-            o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
-            if (XPOOL) {
-              uint32_t* w = reinterpret_cast<uint32_t*>(&o);
-#pragma unroll
-              for (int k = 0; k < 4; ++k) {
-                const uint32_t nb = __shfl_xor_sync(0xffffffffu, w[k], 1);
-                __nv_bfloat162 m = __hmax2(*reinterpret_cast<const __nv_bfloat162*>(&w[k]),
-                                           *reinterpret_cast<const __nv_bfloat162*>(&nb));
-                w[k] = *reinterpret_cast<uint32_t*>(&m);
-              }
+            for (int k = 0; k < 4; ++k) {
+              const uint32_t nb = __shfl_xor_sync(0xffffffffu, w[k], 1);
+              __nv_bfloat162 m = __hmax2(*reinterpret_cast<const __nv_bfloat162*>(&w[k]),
+                                         *reinterpret_cast<const __nv_bfloat162*>(&nb));
+              w[k] = *reinterpret_cast<uint32_t*>(&m);
             }
-            if (pout >= 0)
-              *reinterpret_cast<uint4*>(p.out + (int64_t)(n0 / 8 + c0 / 8 + h) * p.out_cs + pout * 16) = o;
           }
+          if (pout >= 0) *reinterpret_cast<uint4*>(outp + h * p.out_cs + (int64_t)pout * 16) = o;
         }
       }
       ++j;
@@ -1866,7 +1889,7 @@ int weight_stages(const TcLayer& L) {
 
 size_t smem_bytes(const TcLayer& L) {
   if (L.dxf && L.pair)
-    return kDxfWBytes + (size_t)kD2NSA * 16 * 8 * pair_slab_rows(L) + kD2Xchg + 256 + 64 + kSmemReserve;
+    return kDxfWBytes + (size_t)kD2NSA * 16 * 8 * pair_slab_rows(L) + kD2Xchg + 256 + 128 + kSmemReserve;
   if (L.dxf) return kDxfWBytes + kDxfNSA * a_stage_bytes(L) + kDxfXchg + kDxfStage + 32 + kSmemReserve;
   if (L.gather)
     return gather_stages(L) * gather_stage_bytes(L) + (L.wt ? kWtStage : 0) + (size_t)weight_stages(L) * L.nt * 128 +
@@ -2033,7 +2056,19 @@ tdm_status launch_dxf2(const KParams& kp, size_t smem, cudaStream_t s) {
   if (st) return st;
   // persistent: no more pairs than fit at once, so every pair runs from the start
   const int64_t pairs = std::max<int64_t>(1, std::min<int64_t>(kp.total_tiles, dxf2_max_pairs<FP8_OUT, XPOOL>(smem)));
-  kern<<<(unsigned)(2 * pairs), kD2Threads, smem, s>>>(kp, map);
+  PairSched ps;
+  const uint32_t D = (uint32_t)kp.D, D2 = D * D;
+  ps.rows = (uint32_t)kp.rows;
+  ps.step = (uint32_t)(pairs * kD2Out);
+  ps.D3 = D2 * D;
+  ps.rstep = ps.step % ps.D3;
+  ps.zcut = (uint32_t)kp.Do * D2;
+  ps.magic = ((1u << 20) + D - 1) / D;
+  ps.sx = (int)(ps.step % D);
+  ps.sy = (int)(ps.step / D % D);
+  ps.sz = (int)(ps.step / D2 % D);
+  ps.sb = (int)(ps.step / ps.D3);
+  kern<<<(unsigned)(2 * pairs), kD2Threads, smem, s>>>(kp, map, ps);
   TDM_CHECK_LAUNCH("tc_conv_dxf2_kernel");
   return TDM_OK;
 }
@@ -2143,9 +2178,9 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   kp.R = slab_rows(L);
   kp.err = device_error_word();
   if (!kp.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
-  if (L.dxf && L.pair && a.rows > kPairMaxRows) {
-    // slab rows are 32-bit tensor coordinates: larger inputs take the
-    // single-CTA form (same bits)
+  if (L.dxf && L.pair && (a.rows > kPairMaxRows || L.D < 12)) {
+    // slab rows are 32-bit tensor coordinates and the epilogue's row digits
+    // assume D >= 12: other inputs take the single-CTA form (same bits)
     TcLayer L1 = L;
     L1.pair = false;
     return launch_tc_layer(L1, a, s);
