@@ -1307,14 +1307,26 @@ constexpr uint32_t kD2Xchg = 4u * 2u * 4u * 48u * 4u;  // [set][parity][quarter]
 constexpr int kD2Bars = 2 * kD2NSA + 7;
 constexpr int64_t kPairMaxRows = INT32_MAX - (1 << 16);  // slab rows stay below 2^31
 
-// Epilogue row bookkeeping of the pair kernel, fixed per launch: the tile
-// step npairs * 252 rows as digits of the input grid (sx, sy, sz, sb) and
-// modulo D^3 (rstep), the first z-tail row zcut = Do * D^2, and the
-// multiply-shift constant ceil(2^20 / D) for x digits below 256.
+// Work units of the pair kernel: (patch b, block yb of 252 rows of a z plane,
+// segment of zs output planes).  A unit's tiles walk z, so consecutive tiles
+// share two of their three z slabs: a unit of nz tiles loads nz + 2 slabs.
+// nyb blocks cover the rows of a plane that hold outputs (y < Do); nseg
+// segments per column keep every pair busy on small batches.
 struct PairSched {
-  uint32_t rows, step, rstep, D3, zcut, magic;
-  int sx, sy, sz, sb;
+  int nunits, nyb, nseg, zs;
 };
+struct PairUnit {
+  int b, yb, z0, nz;
+};
+__device__ __forceinline__ PairUnit pair_unit(int u, const PairSched& ps, int Do) {
+  const int col = u / ps.nseg, g = u - col * ps.nseg;
+  PairUnit w;
+  w.b = col / ps.nyb;
+  w.yb = col - w.b * ps.nyb;
+  w.z0 = g * ps.zs;
+  w.nz = min(Do, w.z0 + ps.zs) - w.z0;
+  return w;
+}
 
 __device__ __forceinline__ void epi_bar_set(int set) {
   // named barriers 1..4 (0 is __syncthreads), one per epilogue set of 4 warps
@@ -1388,22 +1400,22 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       // halves' bytes), so the MMA issuer waits on one local barrier per stage.
       // The peer loads stage s of use k only after the MMAs of use k - 1 freed
       // it (emptyA, multicast), i.e. after the leader's fullA left that phase.
+      // Slab n of this CTA (counted over all its units) goes to stage
+      // n % NSA; a unit of nz tiles loads its nz + 2 z slabs once.
       const uint32_t fullA_lead = ptx::mapa_shared(fullA, 0);
-      int sa = 0;
-      uint32_t pha = 0;
       int armedA[kD2NSA];
       for (int i = 0; i < kD2NSA; ++i) armedA[i] = -1;
       bool ok = true;
-      for (int64_t t = pair; t < p.total_tiles && ok; t += npairs) {
-        const int64_t m0 = t * kD2Out;
-        if (!tile_has_work(p, m0, kD2Out)) continue;
-        const int64_t s0 = m0 + (int64_t)rank * kDxfSub;
-        for (int zt = 0; zt < 3; ++zt) {
+      uint32_t n = 0;
+      for (int u = (int)pair; u < ps.nunits && ok; u += (int)npairs) {
+        const PairUnit w = pair_unit(u, ps, p.Do);
+        const int64_t base = w.b * (int64_t)plane * p.D + w.yb * kD2Out + (int64_t)rank * kDxfSub + (int64_t)w.z0 * plane;
+        for (int k = 0; k < w.nz + 2; ++k, ++n) {
+          const uint32_t sa = n % kD2NSA, pha = (n / kD2NSA) & 1u;
           if (!TDM_TIMED_WAIT(3, wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER))) { ok = false; break; }
           if (rank == 0) ptx::mbar_arrive_expect_tx(fullA + 8 * sa, 2 * a_stage);
           armedA[sa] = (int)pha;
-          ptx::tma_load_3d_pair(sA_u + sa * a_stage, &tmA, 0, (int)((s0 + zt * plane) >> 1), 0, fullA_lead + 8 * sa);
-          if (++sa == kD2NSA) { sa = 0; pha ^= 1; }
+          ptx::tma_load_3d_pair(sA_u + sa * a_stage, &tmA, 0, (int)((base + k * plane) >> 1), 0, fullA_lead + 8 * sa);
         }
       }
       if (rank == 0) {
@@ -1429,25 +1441,29 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       const uint64_t aDesc0 = ptx::smem_desc(sA_u, lboA, 128), wDesc0 = ptx::smem_desc(sW_u, kDxfN * 16, 128);
       bool ok = wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_MMA) &&
                 wait_or_flag_cluster(peerW, 0, p.err, DEV_TIMEOUT_MMA);
-      int sa = 0;
-      uint32_t pha = 0, j = 0;
+      uint32_t n = 0, j = 0;
 #ifdef TDM_WAIT_STATS
       const long long t_loop0 = clock64();
 #endif
-      for (int64_t t = pair; t < p.total_tiles && ok; t += npairs) {
-        const int64_t m0 = t * kD2Out;
-        if (!tile_has_work(p, m0, kD2Out)) continue;
+      for (int u = (int)pair; u < ps.nunits && ok; u += (int)npairs) {
+        const PairUnit w = pair_unit(u, ps, p.Do);
+        for (int zi = 0; zi < w.nz && ok; ++zi) {
         const uint32_t buf = j & 1u, use = j >> 1;
         if (!TDM_TIMED_WAIT(0, wait_or_flag_cluster(accEmpty + 8 * buf, (use & 1u) ^ 1u, p.err, DEV_TIMEOUT_MMA))) { ok = false; break; }
         ptx::tc_fence_after();
         const uint32_t dbase = tmem + buf * kD2N;
         uint32_t accumulate = 0;
         for (int zt = 0; zt < 3 && ok; ++zt) {
-          if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) {
-            ok = false;
-            break;
+          // tile zi reads slabs zi, zi + 1, zi + 2 of the unit; each slab is
+          // waited for at its first use (the unit's first tile, else zt = 2)
+          const uint32_t sn = n + zi + zt, sa = sn % kD2NSA, pha = (sn / kD2NSA) & 1u;
+          if (zi == 0 || zt == 2) {
+            if (!TDM_TIMED_WAIT(1, wait_or_flag(fullA + 8 * sa, pha, p.err, DEV_TIMEOUT_MMA))) {
+              ok = false;
+              break;
+            }
+            ptx::tc_fence_after();
           }
-          ptx::tc_fence_after();
           const uint64_t aStage = ptx::desc_advance(aDesc0, sa * a_stage);
 #pragma unroll
           for (int dy = 0; dy < 3; ++dy) {
@@ -1460,12 +1476,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
               accumulate = 1;
             }
           }
-          ptx::mma2_commit_both(emptyA + 8 * sa);
-          if (++sa == kD2NSA) { sa = 0; pha ^= 1; }
+          // a slab's last use: zt = 0, or any zt of the unit's last tile
+          if (zt == 0 || zi == w.nz - 1) ptx::mma2_commit_both(emptyA + 8 * sa);
         }
         if (!ok) break;
         ptx::mma2_commit_both(accFull + 8 * buf);
         ++j;
+        }
+        n += w.nz + 2;
       }
 #ifdef TDM_WAIT_STATS
       atomicAdd(&g_wait_stats[6], (unsigned long long)(clock64() - t_loop0));
@@ -1482,54 +1500,20 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
     // this set's columns: channel half set / 2 (the 96 columns of its dx taps),
     // 16 channels at (set % 2) * 16 within each tap's 32
     const uint32_t col0 = (uint32_t)((set >> 1) * kDxfN + (set & 1) * 16);
-    // Row bookkeeping in 32 bits without divisions in the loop (the host sends
-    // inputs of 2^31 - 2^16 rows or more, or grids with D < 12, to the
-    // single-CTA form).  Warp-uniform: the first row s0 = m0 + rank * 126 of
-    // this CTA's half as digits (ux, uy, uz, ub) of the input grid and the
-    // tile's first row within its patch r0 = m0 % D^3, advanced by
-    // npairs * 252 rows per tile step.  Per lane: row s0 + L, whose x digit
-    // ux + L < 256 is split by a multiply-shift (exact for n < 2^20 / D).
-    // The loop constants come from the kernel parameters (PairSched), which
-    // instructions read in place without holding registers.
-    const int D = p.D, Do = p.Do, XO = XPOOL ? p.Do / 2 : p.Do;
-    uint32_t m0 = (uint32_t)(pair * kD2Out), r0 = m0 % ps.D3, s0 = m0 + rank * kDxfSub;
-    int ux = (int)(s0 % D), uy = (int)(s0 / D % D), uz = (int)(s0 / (D * D) % D), ub = (int)(s0 / ps.D3);
+    const int Do = p.Do, XO = XPOOL ? p.Do / 2 : p.Do;
     uint8_t* const outp = p.out + (int64_t)(n0 / (FP8_OUT ? 16 : 8)) * p.out_cs;
     uint32_t j = 0;
-    for (int t = (int)pair; t < (int)p.total_tiles; t += (int)npairs) {
-      // the same test as tile_has_work, from r0
-      const bool work = m0 < ps.rows && (p.nyx == 1 || !(r0 >= ps.zcut && r0 + kD2Out <= ps.D3));
-      // this lane's output offset (rows L < 126 of this CTA's half; x-pooled:
-      // the even rows hold the pair maxima), or -1
-      int pout = -1;
-      {
-        const int n = ux + L, cy = (int)(((uint32_t)n * ps.magic) >> 20), x = n - cy * D;
-        int y = uy + cy, c = y >= D;
-        y -= c ? D : 0;
-        int z = uz + c;
-        c = z >= D;
-        z -= c ? D : 0;
-        const int bb = ub + c;
-        if (L < kDxfSub && s0 + L < ps.rows && x < Do && y < Do && z < Do && (!XPOOL || (x & 1) == 0))
-          pout = ((bb * Do + z) * Do + y) * XO + (XPOOL ? x / 2 : x);
-      }
-      {  // advance to tile t + npairs
-        m0 += ps.step;
-        s0 += ps.step;
-        r0 += ps.rstep;
-        r0 -= r0 >= ps.D3 ? ps.D3 : 0;
-        ux += ps.sx;
-        int c = ux >= D;
-        ux -= c ? D : 0;
-        uy += ps.sy + c;
-        c = uy >= D;
-        uy -= c ? D : 0;
-        uz += ps.sz + c;
-        c = uz >= D;
-        uz -= c ? D : 0;
-        ub += ps.sb + c;
-      }
-      if (!work) continue;
+    bool stop = false;
+    for (int u = (int)pair; u < ps.nunits && !stop; u += (int)npairs) {
+      const PairUnit w = pair_unit(u, ps, Do);
+      // this lane's row within a z plane (the same for every tile of the
+      // unit) and its output offset at z = 0, or -1 (rows L < 126 of this
+      // CTA's half, x, y < Do; x-pooled: the even rows hold the pair maxima)
+      const int pp = w.yb * kD2Out + (int)rank * kDxfSub + L, y = pp / p.D, x = pp - y * p.D;
+      const bool lane_ok = L < kDxfSub && x < Do && y < Do && (!XPOOL || (x & 1) == 0);
+      const int pbase = ((w.b * Do + w.z0) * Do + y) * XO + (XPOOL ? x / 2 : x);
+      for (int zi = 0; zi < w.nz; ++zi) {
+      const int pout = lane_ok ? pbase + zi * Do * XO : -1;
       const uint32_t buf = j & 1u, use = j >> 1;
       const int got = __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0);
       int* vote = sVote + (set * 2 + (j & 1u)) * 4;
@@ -1570,7 +1554,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
         }
       }
       epi_bar_set(set);  // A
-      if (!(vote[0] && vote[1] && vote[2] && vote[3])) break;
+      if (!(vote[0] && vote[1] && vote[2] && vote[3])) {
+        stop = true;
+        break;
+      }
       const float* xn = xs + ((q + 1) & 3) * 48;  // next quarter (q = 3: rows >= 126 only)
       const bool l31 = lane == 31, l30 = lane == 30;
       float v[16];
@@ -1632,6 +1619,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
         }
       }
       ++j;
+      }
     }
   }
   ptx::tc_fence_before();
@@ -2055,19 +2043,18 @@ tdm_status launch_dxf2(const KParams& kp, size_t smem, cudaStream_t s) {
   tdm_status st = slab_tensor_map(kp, &map);
   if (st) return st;
   // persistent: no more pairs than fit at once, so every pair runs from the start
-  const int64_t pairs = std::max<int64_t>(1, std::min<int64_t>(kp.total_tiles, dxf2_max_pairs<FP8_OUT, XPOOL>(smem)));
+  const int max_pairs = dxf2_max_pairs<FP8_OUT, XPOOL>(smem);
+  const int64_t D3 = (int64_t)kp.D * kp.D * kp.D, B = kp.rows / D3;
   PairSched ps;
-  const uint32_t D = (uint32_t)kp.D, D2 = D * D;
-  ps.rows = (uint32_t)kp.rows;
-  ps.step = (uint32_t)(pairs * kD2Out);
-  ps.D3 = D2 * D;
-  ps.rstep = ps.step % ps.D3;
-  ps.zcut = (uint32_t)kp.Do * D2;
-  ps.magic = ((1u << 20) + D - 1) / D;
-  ps.sx = (int)(ps.step % D);
-  ps.sy = (int)(ps.step / D % D);
-  ps.sz = (int)(ps.step / D2 % D);
-  ps.sb = (int)(ps.step / ps.D3);
+  ps.nyb = (kp.Do * kp.D + kD2Out - 1) / kD2Out;
+  const int64_t cols = B * ps.nyb;
+  // split the z walk only when the columns alone leave pairs idle
+  const int64_t want = (4 * (int64_t)max_pairs + cols - 1) / cols;
+  const int nseg0 = (int)std::max<int64_t>(1, std::min<int64_t>(kp.Do, want));
+  ps.zs = (kp.Do + nseg0 - 1) / nseg0;
+  ps.nseg = (kp.Do + ps.zs - 1) / ps.zs;
+  ps.nunits = (int)(cols * ps.nseg);
+  const int64_t pairs = std::max<int64_t>(1, std::min<int64_t>(ps.nunits, max_pairs));
   kern<<<(unsigned)(2 * pairs), kD2Threads, smem, s>>>(kp, map, ps);
   TDM_CHECK_LAUNCH("tc_conv_dxf2_kernel");
   return TDM_OK;
@@ -2178,9 +2165,10 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   kp.R = slab_rows(L);
   kp.err = device_error_word();
   if (!kp.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
-  if (L.dxf && L.pair && (a.rows > kPairMaxRows || L.D < 12)) {
-    // slab rows are 32-bit tensor coordinates and the epilogue's row digits
-    // assume D >= 12: other inputs take the single-CTA form (same bits)
+  if (L.dxf && L.pair &&
+      (a.rows > kPairMaxRows || a.rows % ((int64_t)L.D * L.D * L.D) != 0)) {
+    // slab rows are 32-bit tensor coordinates and units are whole patches:
+    // other inputs take the single-CTA form (same bits)
     TcLayer L1 = L;
     L1.pair = false;
     return launch_tc_layer(L1, a, s);
