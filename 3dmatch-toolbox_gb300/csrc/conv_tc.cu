@@ -1647,6 +1647,8 @@ constexpr int kC1Rows = 512;                          // rows per tile (4 sub-ti
 constexpr int kC1NSA = 3;                             // A stages
 constexpr uint32_t kC1Stage = 4u * kC1Rows * 16u;     // 32 KB
 constexpr uint32_t kC1W = 4u * 64u * 16u;             // weights: 4 chunks x 64 rows x 16 B
+constexpr int kC1TilesPerPatch = (21952 + kC1Rows - 1) / kC1Rows;  // 43
+constexpr int kC1PlaneSpan = 4 * 900;                 // floats: the <= 4 input z planes of a tile
 
 struct C1Params {
   const float* patches;
@@ -1664,12 +1666,14 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
   constexpr uint32_t ACC = 4 * 64;  // one buffer: 4 sub-tiles x N 64
   uint8_t* sW = smem;
   uint8_t* sA = smem + kC1W;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sA + kC1NSA * kC1Stage);
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * kC1NSA + 6);
+  float* sP = reinterpret_cast<float*>(sA + kC1NSA * kC1Stage);  // [2][kC1PlaneSpan] input planes
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sP + 2 * kC1PlaneSpan);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * kC1NSA + 8);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (!__syncthreads_and(aborted(p.err) ? 0 : 1)) return;
   const uint32_t fullA = ptx::smem_u32(bars), emptyA = fullA + 8 * kC1NSA;
-  const uint32_t wfull = emptyA + 8 * kC1NSA, accFull = wfull + 8, accEmpty = accFull + 16, done = accEmpty + 16;
+  const uint32_t wfull = emptyA + 8 * kC1NSA, accFull = wfull + 8, accEmpty = accFull + 16, done = accEmpty + 16,
+                 fullP = done + 8;
   if (threadIdx.x == 0) {
     for (int i = 0; i < kC1NSA; ++i) {
       ptx::mbar_init(fullA + 8 * i, 32 * kC1Prod);  // every producer thread arrives
@@ -1678,6 +1682,7 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
     ptx::mbar_init(wfull, 1);
     for (int i = 0; i < 2; ++i) { ptx::mbar_init(accFull + 8 * i, 1); ptx::mbar_init(accEmpty + 8 * i, 4); }
     ptx::mbar_init(done, 1);
+    for (int i = 0; i < 2; ++i) ptx::mbar_init(fullP + 8 * i, 1);
     ptx::fence_barrier_init();
     ptx::fence_proxy_async_smem();
   }
@@ -1693,41 +1698,82 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
 
   if (warp < kC1Prod) {
     // ---------------- producers: im2col rows into the stages ----------------
+    // A tile is 512 rows of one patch (43 tiles per patch, the last one 448
+    // rows).  Its rows need at most four consecutive z planes of the 30^3
+    // patch (14.4 KB): thread 0 copies them into shared memory one tile ahead
+    // (two buffers), and the 27 taps of each row are read from there.
     const int pt = threadIdx.x;  // 0 .. 127
+    const uint32_t sP_u = ptx::smem_u32(sP);
     if (pt == 0) {
       ptx::mbar_arrive_expect_tx(wfull, kC1W);
       ptx::bulk_g2s(sW_u, p.wpk, kC1W, wfull);
     }
+    auto planes_copy = [&](int64_t t, int buf) {  // thread 0: the tile's input planes
+      const int64_t b = t / kC1TilesPerPatch;
+      const int r0 = (int)(t - b * kC1TilesPerPatch) * kC1Rows, r1 = min(21952, r0 + kC1Rows);
+      const int zlo = r0 / 784, np = (r1 - 1) / 784 - zlo + 3;
+      const uint32_t bytes = (uint32_t)np * 900u * 4u;
+      ptx::mbar_arrive_expect_tx(fullP + 8 * buf, bytes);
+      ptx::bulk_g2s(sP_u + (uint32_t)buf * kC1PlaneSpan * 4u, p.patches + b * 27000 + (int64_t)zlo * 900, bytes,
+                    fullP + 8 * buf);
+    };
     int sa = 0;
     uint32_t pha = 0;
     bool ok = true;
+    int64_t issued = -1, waited = -1;  // thread 0: local tile index of the last plane copy issued / waited for
     constexpr int kRowsPerThread = kC1Rows / (32 * kC1Prod);
-    for (int64_t t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
-      // all 27 x 4 loads of this thread's rows in flight at once, issued
-      // before the wait for a free stage
+    if (pt == 0 && (int64_t)blockIdx.x < p.tiles) {
+      planes_copy(blockIdx.x, 0);
+      issued = 0;
+    }
+    uint32_t k = 0;
+    for (int64_t t = blockIdx.x; t < p.tiles && ok; t += gridDim.x, ++k) {
+      const int buf = (int)(k & 1u);
+      if (pt == 0 && t + gridDim.x < p.tiles) {
+        planes_copy(t + gridDim.x, buf ^ 1);
+        issued = k + 1;
+      }
+      const int64_t b = t / kC1TilesPerPatch;
+      const int r0 = (int)(t - b * kC1TilesPerPatch) * kC1Rows, nrows = min(kC1Rows, 21952 - r0);
+      const int zlo = r0 / 784;
+      const bool okP = wait_or_flag(fullP + 8 * buf, (k >> 1) & 1u, p.err, DEV_TIMEOUT_PRODUCER);
+      if (pt == 0 && okP) waited = k;
+      const float* sp = sP + buf * kC1PlaneSpan;
       float v[kRowsPerThread][27];
 #pragma unroll
-      for (int k = 0; k < kRowsPerThread; ++k) {
-        int64_t row = t * kC1Rows + pt + 32 * kC1Prod * k;
-        row = row < p.rows ? row : p.rows - 1;  // rows past the end load a valid row and store zeros
-        const int64_t b = row / 21952;
-        const int q = (int)(row - b * 21952);
-        const int z = q / 784, y = (q / 28) % 28, x = q % 28;
-        const float* src = p.patches + b * 27000 + z * 900 + y * 30 + x;
+      for (int kr = 0; kr < kRowsPerThread; ++kr) {
+        // rows past the tile's end read a valid row and store zeros
+        const int r = r0 + min(pt + 32 * kC1Prod * kr, nrows - 1);
+        const int z = r / 784 - zlo, y = (r / 28) % 28, x = r % 28;
+        const float* src = sp + z * 900 + y * 30 + x;
 #pragma unroll
-        for (int tp = 0; tp < 27; ++tp) v[k][tp] = __ldg(src + (tp / 9) * 900 + ((tp / 3) % 3) * 30 + (tp % 3));
+        for (int tp = 0; tp < 27; ++tp) v[kr][tp] = src[(tp / 9) * 900 + ((tp / 3) % 3) * 30 + (tp % 3)];
       }
-      if (!wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER)) { ok = false; break; }
+      const bool okA = wait_or_flag(emptyA + 8 * sa, pha ^ 1, p.err, DEV_TIMEOUT_PRODUCER);
+      // Every producer has read this plane buffer (thread 0 refills it next
+      // tile), and all 128 learn together whether both waits succeeded, so
+      // they leave the loop together and this barrier is always met.
+      int all;
+      asm volatile(
+          "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.and.pred q, 1, %2, p;\n\t"
+          "selp.s32 %0, 1, 0, q;\n\t}"
+          : "=r"(all)
+          : "r"((okP && okA) ? 1 : 0), "r"(32 * kC1Prod)
+          : "memory");
+      if (!all) {
+        ok = false;
+        break;
+      }
       uint8_t* st = sA + sa * kC1Stage;
 #pragma unroll
-      for (int k = 0; k < kRowsPerThread; ++k) {
-        const int r = pt + 32 * kC1Prod * k;
-        const float keep = t * kC1Rows + r < p.rows ? 1.0f : 0.0f;
+      for (int kr = 0; kr < kRowsPerThread; ++kr) {
+        const int r = pt + 32 * kC1Prod * kr;
+        const float keep = r < nrows ? 1.0f : 0.0f;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           float f[8];
 #pragma unroll
-          for (int e = 0; e < 8; ++e) f[e] = 8 * j + e < 27 ? v[k][8 * j + e] * keep : 0.0f;
+          for (int e = 0; e < 8; ++e) f[e] = 8 * j + e < 27 ? v[kr][8 * j + e] * keep : 0.0f;
           uint4 o;
           o.x = pack_bf16x2(f[0], f[1]);
           o.y = pack_bf16x2(f[2], f[3]);
@@ -1740,7 +1786,18 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
       mbar_arrive(fullA + 8 * sa);
       if (++sa == kC1NSA) { sa = 0; pha ^= 1; }
     }
-    if (pt == 0) wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_PRODUCER);
+    if (pt == 0) {
+      if (issued > waited) {
+        // a plane copy issued for a tile the loop did not reach: let it land
+        // (bounded); after an abort give any copy in flight 200 us
+        const uint32_t kk = (uint32_t)issued;
+        if (!wait_or_flag(fullP + 8 * (kk & 1u), (kk >> 1) & 1u, p.err, DEV_TIMEOUT_PRODUCER)) {
+          const uint64_t t0 = ptx::globaltimer_ns();
+          while (ptx::globaltimer_ns() - t0 < 200000ull) __nanosleep(1000);
+        }
+      }
+      wait_or_flag(wfull, 0, p.err, DEV_TIMEOUT_PRODUCER);
+    }
   } else if (warp == kC1Prod) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
@@ -1795,8 +1852,10 @@ __global__ void __launch_bounds__(kC1Threads, 1) tc_conv1_kernel(const C1Params 
       ptx::tc_fence_after();
 #pragma unroll 1
       for (int i = 0; i < 4; ++i) {
-        const int64_t row = t * kC1Rows + i * 128 + q * 32 + lane;
-        const bool valid = row < p.rows;
+        const int64_t b = t / kC1TilesPerPatch;
+        const int rp = (int)(t - b * kC1TilesPerPatch) * kC1Rows + i * 128 + q * 32 + lane;  // row in the patch
+        const bool valid = rp < 21952;
+        const int64_t row = b * 21952 + rp;
         uint32_t r[4][16];  // the row's 64 accumulators: four loads, one wait
 #pragma unroll
         for (int k = 0; k < 4; ++k)
@@ -2088,11 +2147,12 @@ tdm_status launch_conv1_tc(const float* patches, int B, const TcLayer& L, uint8_
   p.bias = L.bias;
   p.out = out;
   p.out_cs = out_cs;
-  p.tiles = (p.rows + kC1Rows - 1) / kC1Rows;
+  p.tiles = (int64_t)B * kC1TilesPerPatch;
   p.err = device_error_word();
   if (!p.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
   if (p.rows == 0) return TDM_OK;
-  const size_t smem = kC1W + kC1NSA * kC1Stage + 256;
+  TDM_REQUIRE((reinterpret_cast<uintptr_t>(patches) & 15) == 0, "conv1: patches must be 16-byte aligned");
+  const size_t smem = kC1W + kC1NSA * kC1Stage + 2 * kC1PlaneSpan * 4 + 256;
   cudaError_t attr_err = raise_smem_cap(reinterpret_cast<const void*>(tc_conv1_kernel), (int)kSmemLimit);
   if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv1_kernel)");
   const int64_t grid = std::min<int64_t>(p.tiles, sm_count());
