@@ -213,8 +213,9 @@ __global__ __launch_bounds__(256) void pool_f32_kernel(const float* __restrict__
 
 // Same pool on the BF16 chunk-planar layout (8 channels per 16-byte row).
 // XP: the input is already max-pooled along x (x extent D/2, written so by
-// the dx-fused conv2), so only the four (z, y) taps remain.
-template <bool XP>
+// the dx-fused conv2), so only the four (z, y) taps remain; ZP (with XP):
+// also along z (the CTA-pair conv2), so only the two y taps remain.
+template <bool XP, bool ZP = false>
 __global__ __launch_bounds__(256) void pool_c8_kernel(const uint8_t* __restrict__ in, int64_t in_cs, int D,
                                                       int nchunks, int64_t n_out, uint8_t* __restrict__ out,
                                                       int64_t out_cs) {
@@ -229,13 +230,14 @@ __global__ __launch_bounds__(256) void pool_c8_kernel(const uint8_t* __restrict_
   int z = r / (Do * Do), y = (r / Do) % Do, x = r % Do;
   __nv_bfloat162 best[4];
   const uint8_t* src = in + (int64_t)j * in_cs;
-  constexpr int TAPS = XP ? 4 : 8;
+  constexpr int TAPS = ZP ? 2 : XP ? 4 : 8;
+  const int ZW = ZP ? Do : D;
 #pragma unroll
   for (int t = 0; t < TAPS; ++t) {
-    const int zz = XP ? 2 * z + (t >> 1) : 2 * z + (t >> 2);
-    const int yy = XP ? 2 * y + (t & 1) : 2 * y + ((t >> 1) & 1);
+    const int zz = ZP ? z : XP ? 2 * z + (t >> 1) : 2 * z + (t >> 2);
+    const int yy = ZP ? 2 * y + t : XP ? 2 * y + (t & 1) : 2 * y + ((t >> 1) & 1);
     const int xx = XP ? x : 2 * x + (t & 1);
-    uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (((b * D + zz) * D + yy) * XW + xx) * 16));
+    uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (((b * ZW + zz) * D + yy) * XW + xx) * 16));
     __nv_bfloat162 e[4];
     memcpy(e, &v, 16);
 #pragma unroll
@@ -249,7 +251,7 @@ __global__ __launch_bounds__(256) void pool_c8_kernel(const uint8_t* __restrict_
 // Same pool on the E4M3 chunk-planar layout (16 channels per 16-byte row).
 // Inputs are ReLU outputs (>= 0), whose E4M3 bytes order like the values, so
 // a byte-wise unsigned max is the max-pool.
-template <bool XP>
+template <bool XP, bool ZP = false>
 __global__ __launch_bounds__(256) void pool_c16_u8_kernel(const uint8_t* __restrict__ in, int64_t in_cs, int D,
                                                           int nchunks, int64_t n_out, uint8_t* __restrict__ out,
                                                           int64_t out_cs) {
@@ -264,13 +266,14 @@ __global__ __launch_bounds__(256) void pool_c16_u8_kernel(const uint8_t* __restr
   int z = r / (Do * Do), y = (r / Do) % Do, x = r % Do;
   const uint8_t* src = in + (int64_t)j * in_cs;
   uint4 best = make_uint4(0, 0, 0, 0);
-  constexpr int TAPS = XP ? 4 : 8;
+  constexpr int TAPS = ZP ? 2 : XP ? 4 : 8;
+  const int ZW = ZP ? Do : D;
 #pragma unroll
   for (int t = 0; t < TAPS; ++t) {
-    const int zz = XP ? 2 * z + (t >> 1) : 2 * z + (t >> 2);
-    const int yy = XP ? 2 * y + (t & 1) : 2 * y + ((t >> 1) & 1);
+    const int zz = ZP ? z : XP ? 2 * z + (t >> 1) : 2 * z + (t >> 2);
+    const int yy = ZP ? 2 * y + t : XP ? 2 * y + (t & 1) : 2 * y + ((t >> 1) & 1);
     const int xx = XP ? x : 2 * x + (t & 1);
-    uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (((b * D + zz) * D + yy) * XW + xx) * 16));
+    uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (((b * ZW + zz) * D + yy) * XW + xx) * 16));
     best.x = __vmaxu4(best.x, v.x);
     best.y = __vmaxu4(best.y, v.y);
     best.z = __vmaxu4(best.z, v.z);
@@ -282,11 +285,14 @@ __global__ __launch_bounds__(256) void pool_c16_u8_kernel(const uint8_t* __restr
 }  // namespace
 
 tdm_status launch_pool_c16_u8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out,
-                              int64_t out_cs, cudaStream_t s, bool x_pooled) {
+                              int64_t out_cs, cudaStream_t s, bool x_pooled, bool z_pooled) {
   int Do = D / 2;
   int64_t n_out = (int64_t)B * Do * Do * Do;
   int64_t n = n_out * nchunks;
-  if (x_pooled)
+  TDM_REQUIRE(!z_pooled || x_pooled, "pool: a z-pooled input is x-pooled too");
+  if (z_pooled)
+    pool_c16_u8_kernel<true, true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, in_cs, D, nchunks, n_out, out, out_cs);
+  else if (x_pooled)
     pool_c16_u8_kernel<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, in_cs, D, nchunks, n_out, out, out_cs);
   else
     pool_c16_u8_kernel<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, in_cs, D, nchunks, n_out, out, out_cs);
@@ -330,11 +336,14 @@ tdm_status launch_pool_f32(const float* in, int B, int D, int C, float* out, cud
 }
 
 tdm_status launch_pool_c8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out, int64_t out_cs,
-                          cudaStream_t s, bool x_pooled) {
+                          cudaStream_t s, bool x_pooled, bool z_pooled) {
   int Do = D / 2;
   int64_t n_out = (int64_t)B * Do * Do * Do;
   int64_t n = n_out * nchunks;
-  if (x_pooled)
+  TDM_REQUIRE(!z_pooled || x_pooled, "pool: a z-pooled input is x-pooled too");
+  if (z_pooled)
+    pool_c8_kernel<true, true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, in_cs, D, nchunks, n_out, out, out_cs);
+  else if (x_pooled)
     pool_c8_kernel<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, in_cs, D, nchunks, n_out, out, out_cs);
   else
     pool_c8_kernel<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, in_cs, D, nchunks, n_out, out, out_cs);

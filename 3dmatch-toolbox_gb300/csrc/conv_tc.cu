@@ -1333,7 +1333,7 @@ __device__ __forceinline__ void epi_bar_set(int set) {
   asm volatile("bar.sync %0, 128;" ::"r"(set + 1) : "memory");
 }
 
-template <bool FP8_OUT, bool XPOOL>
+template <bool FP8_OUT, bool XPOOL, bool ZPOOL>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_conv_dxf2_kernel(const KParams p,
                                                                                           const __grid_constant__ CUtensorMap tmA,
                                                                                           const PairSched ps) {
@@ -1500,10 +1500,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
     // this set's columns: channel half set / 2 (the 96 columns of its dx taps),
     // 16 channels at (set % 2) * 16 within each tap's 32
     const uint32_t col0 = (uint32_t)((set >> 1) * kDxfN + (set & 1) * 16);
-    const int Do = p.Do, XO = XPOOL ? p.Do / 2 : p.Do;
+    static_assert(!ZPOOL || XPOOL, "the z-pair max comes with the x-pair max");
+    const int Do = p.Do, XO = XPOOL ? p.Do / 2 : p.Do, ZO = ZPOOL ? p.Do / 2 : p.Do;
     uint8_t* const outp = p.out + (int64_t)(n0 / (FP8_OUT ? 16 : 8)) * p.out_cs;
     uint32_t j = 0;
     bool stop = false;
+    // z-pooled: units start on even z with an even number of tiles, and the
+    // same warp drains tiles z and z + 1 one after the other, so it keeps the
+    // even tile's packed output here and stores the max with the odd one
+    uint4 zkeep[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
     for (int u = (int)pair; u < ps.nunits && !stop; u += (int)npairs) {
       const PairUnit w = pair_unit(u, ps, Do);
       // this lane's row within a z plane (the same for every tile of the
@@ -1511,9 +1516,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       // CTA's half, x, y < Do; x-pooled: the even rows hold the pair maxima)
       const int pp = w.yb * kD2Out + (int)rank * kDxfSub + L, y = pp / p.D, x = pp - y * p.D;
       const bool lane_ok = L < kDxfSub && x < Do && y < Do && (!XPOOL || (x & 1) == 0);
-      const int pbase = ((w.b * Do + w.z0) * Do + y) * XO + (XPOOL ? x / 2 : x);
+      const int pbase = ((w.b * ZO + (ZPOOL ? w.z0 / 2 : w.z0)) * Do + y) * XO + (XPOOL ? x / 2 : x);
       for (int zi = 0; zi < w.nz; ++zi) {
-      const int pout = lane_ok ? pbase + zi * Do * XO : -1;
+      const int pout = lane_ok ? pbase + (ZPOOL ? zi / 2 : zi) * Do * XO : -1;
+      const bool zstore = !ZPOOL || (zi & 1);  // z-pooled: the odd tile of each z pair stores
       const uint32_t buf = j & 1u, use = j >> 1;
       const int got = __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0);
       int* vote = sVote + (set * 2 + (j & 1u)) * 4;
@@ -1560,17 +1566,19 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       }
       const float* xn = xs + ((q + 1) & 3) * 48;  // next quarter (q = 3: rows >= 126 only)
       const bool l31 = lane == 31, l30 = lane == 30;
-      float v[16];
+      // the 16 outputs, packed four channels at a time as they are made
+      // (E4M3: one word per four, BF16: two), which keeps few registers live
+      uint32_t pk[FP8_OUT ? 4 : 8];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        // neighbour-quarter values and biases: broadcast shared-memory loads,
-        // four channels at a time
+        // neighbour-quarter values and biases: broadcast shared-memory loads
         const float4 u = reinterpret_cast<const float4*>(xn)[k];
         const float4 w = reinterpret_cast<const float4*>(xn + 16)[k];
         const float4 zz = reinterpret_cast<const float4*>(xn + 32)[k];
         const float4 c = reinterpret_cast<const float4*>(sBias + n0)[k];
         const float nb1[4] = {u.x, u.y, u.z, u.w}, nb2a[4] = {w.x, w.y, w.z, w.w};
         const float nb2b[4] = {zz.x, zz.y, zz.z, zz.w}, bi[4] = {c.x, c.y, c.z, c.w};
+        float v[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int e = 4 * k + i;
@@ -1579,32 +1587,41 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
           s1 = l31 ? nb1[i] : s1;
           s2 = l31 ? nb2b[i] : (l30 ? nb2a[i] : s2);
           const float a = ((__uint_as_float(r0v[e]) + s1) + s2) + bi[i];
-          v[e] = p.relu ? fmaxf(a, 0.0f) : a;
+          v[i] = p.relu ? fmaxf(a, 0.0f) : a;
+        }
+        if (FP8_OUT) {
+          pk[k] = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
+        } else {
+          pk[2 * k] = pack_bf16x2(v[0], v[1]);
+          pk[2 * k + 1] = pack_bf16x2(v[2], v[3]);
         }
       }
       // stores straight from registers: chunk-planar output, 16 B per row
       // and chunk; a warp's even lanes write consecutive pooled rows
       if (FP8_OUT) {
-        uint4 o;
-        o.x = pack_e4m3x4(v[0] * p.out_qinv, v[1] * p.out_qinv, v[2] * p.out_qinv, v[3] * p.out_qinv);
-        o.y = pack_e4m3x4(v[4] * p.out_qinv, v[5] * p.out_qinv, v[6] * p.out_qinv, v[7] * p.out_qinv);
-        o.z = pack_e4m3x4(v[8] * p.out_qinv, v[9] * p.out_qinv, v[10] * p.out_qinv, v[11] * p.out_qinv);
-        o.w = pack_e4m3x4(v[12] * p.out_qinv, v[13] * p.out_qinv, v[14] * p.out_qinv, v[15] * p.out_qinv);
+        uint4 o = make_uint4(pk[0], pk[1], pk[2], pk[3 % (FP8_OUT ? 4 : 8)]);
         if (XPOOL) {
           o.x = __vmaxu4(o.x, __shfl_xor_sync(0xffffffffu, o.x, 1));
           o.y = __vmaxu4(o.y, __shfl_xor_sync(0xffffffffu, o.y, 1));
           o.z = __vmaxu4(o.z, __shfl_xor_sync(0xffffffffu, o.z, 1));
           o.w = __vmaxu4(o.w, __shfl_xor_sync(0xffffffffu, o.w, 1));
         }
-        if (pout >= 0) *reinterpret_cast<uint4*>(outp + (int64_t)pout * 16) = o;
+        if (ZPOOL) {
+          if (zi & 1) {
+            o.x = __vmaxu4(o.x, zkeep[0].x);
+            o.y = __vmaxu4(o.y, zkeep[0].y);
+            o.z = __vmaxu4(o.z, zkeep[0].z);
+            o.w = __vmaxu4(o.w, zkeep[0].w);
+          } else {
+            zkeep[0] = o;
+          }
+        }
+        if (zstore && pout >= 0) *reinterpret_cast<uint4*>(outp + (int64_t)pout * 16) = o;
       } else {
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          uint4 o;
-          o.x = pack_bf16x2(v[8 * h + 0], v[8 * h + 1]);
-          o.y = pack_bf16x2(v[8 * h + 2], v[8 * h + 3]);
-          o.z = pack_bf16x2(v[8 * h + 4], v[8 * h + 5]);
-          o.w = pack_bf16x2(v[8 * h + 6], v[8 * h + 7]);
+          uint4 o = make_uint4(pk[(4 * h) % (FP8_OUT ? 4 : 8)], pk[(4 * h + 1) % (FP8_OUT ? 4 : 8)],
+                               pk[(4 * h + 2) % (FP8_OUT ? 4 : 8)], pk[(4 * h + 3) % (FP8_OUT ? 4 : 8)]);
           if (XPOOL) {
             uint32_t* w = reinterpret_cast<uint32_t*>(&o);
 #pragma unroll
@@ -1615,7 +1632,21 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
               w[k] = *reinterpret_cast<uint32_t*>(&m);
             }
           }
-          if (pout >= 0) *reinterpret_cast<uint4*>(outp + h * p.out_cs + (int64_t)pout * 16) = o;
+          if (ZPOOL) {
+            if (zi & 1) {
+              uint32_t* w = reinterpret_cast<uint32_t*>(&o);
+              const uint32_t* kv = reinterpret_cast<const uint32_t*>(&zkeep[h]);
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                __nv_bfloat162 m = __hmax2(*reinterpret_cast<const __nv_bfloat162*>(&w[k]),
+                                           *reinterpret_cast<const __nv_bfloat162*>(&kv[k]));
+                w[k] = *reinterpret_cast<uint32_t*>(&m);
+              }
+            } else {
+              zkeep[h] = o;
+            }
+          }
+          if (zstore && pout >= 0) *reinterpret_cast<uint4*>(outp + h * p.out_cs + (int64_t)pout * 16) = o;
         }
       }
       ++j;
@@ -2027,7 +2058,7 @@ bool gather_tile_built(int nt, int msub) {
 
 // CTA pairs of the pair form that can be resident at once on this device
 // (clusters need both CTAs on one GPC; one CTA per SM), cached per device.
-template <bool FP8_OUT, bool XPOOL>
+template <bool FP8_OUT, bool XPOOL, bool ZPOOL>
 int dxf2_max_pairs(size_t smem) {
   static std::mutex mu;
   static std::map<int, int> cache;
@@ -2048,7 +2079,7 @@ int dxf2_max_pairs(size_t smem) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, tc_conv_dxf2_kernel<FP8_OUT, XPOOL>, &cfg) != cudaSuccess || n <= 0) {
+  if (cudaOccupancyMaxActiveClusters(&n, tc_conv_dxf2_kernel<FP8_OUT, XPOOL, ZPOOL>, &cfg) != cudaSuccess || n <= 0) {
     cudaGetLastError();
     n = device_sm_count() / 2;
   }
@@ -2093,16 +2124,16 @@ tdm_status slab_tensor_map(const KParams& kp, CUtensorMap* map) {
   return TDM_OK;
 }
 
-template <bool FP8_OUT, bool XPOOL>
+template <bool FP8_OUT, bool XPOOL, bool ZPOOL>
 tdm_status launch_dxf2(const KParams& kp, size_t smem, cudaStream_t s) {
-  auto kern = tc_conv_dxf2_kernel<FP8_OUT, XPOOL>;
+  auto kern = tc_conv_dxf2_kernel<FP8_OUT, XPOOL, ZPOOL>;
   cudaError_t attr_err = raise_smem_cap(reinterpret_cast<const void*>(kern), (int)kSmemLimit);
   if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_dxf2_kernel)");
   CUtensorMap map;
   tdm_status st = slab_tensor_map(kp, &map);
   if (st) return st;
   // persistent: no more pairs than fit at once, so every pair runs from the start
-  const int max_pairs = dxf2_max_pairs<FP8_OUT, XPOOL>(smem);
+  const int max_pairs = dxf2_max_pairs<FP8_OUT, XPOOL, ZPOOL>(smem);
   const int64_t D3 = (int64_t)kp.D * kp.D * kp.D, B = kp.rows / D3;
   PairSched ps;
   ps.nyb = (kp.Do * kp.D + kD2Out - 1) / kD2Out;
@@ -2111,6 +2142,7 @@ tdm_status launch_dxf2(const KParams& kp, size_t smem, cudaStream_t s) {
   const int64_t want = (4 * (int64_t)max_pairs + cols - 1) / cols;
   const int nseg0 = (int)std::max<int64_t>(1, std::min<int64_t>(kp.Do, want));
   ps.zs = (kp.Do + nseg0 - 1) / nseg0;
+  if (ZPOOL) ps.zs += ps.zs & 1;  // whole z pairs per unit (Do is even)
   ps.nseg = (kp.Do + ps.zs - 1) / ps.zs;
   ps.nunits = (int)(cols * ps.nseg);
   const int64_t pairs = std::max<int64_t>(1, std::min<int64_t>(ps.nunits, max_pairs));
@@ -2201,6 +2233,10 @@ bool tc_layer_fits(const TcLayer& L) {
          smem_bytes(L) <= kSmemLimit;
 }
 
+bool tc_pair_form_applies(const TcLayer& L, int64_t rows) {
+  return L.dxf && L.pair && rows <= kPairMaxRows && rows % ((int64_t)L.D * L.D * L.D) == 0;
+}
+
 tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   KParams kp;
   kp.act = a.act;
@@ -2225,10 +2261,10 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   kp.R = slab_rows(L);
   kp.err = device_error_word();
   if (!kp.err) return fail(TDM_ERR_DEVICE, "device error word unavailable");
-  if (L.dxf && L.pair &&
-      (a.rows > kPairMaxRows || a.rows % ((int64_t)L.D * L.D * L.D) != 0)) {
+  if (L.dxf && L.pair && !tc_pair_form_applies(L, a.rows)) {
     // slab rows are 32-bit tensor coordinates and units are whole patches:
     // other inputs take the single-CTA form (same bits)
+    TDM_REQUIRE(!a.zpool, "tc layer: the z-pair max needs the CTA-pair form");
     TcLayer L1 = L;
     L1.pair = false;
     return launch_tc_layer(L1, a, s);
@@ -2246,8 +2282,13 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
     kp.nsb = 0;
     kp.total_tiles = (a.rows + kD2Out - 1) / kD2Out;
     const size_t smem = smem_bytes(L);
-    if (L.fp8_out) return a.xpool ? launch_dxf2<true, true>(kp, smem, s) : launch_dxf2<true, false>(kp, smem, s);
-    return a.xpool ? launch_dxf2<false, true>(kp, smem, s) : launch_dxf2<false, false>(kp, smem, s);
+    TDM_REQUIRE(!a.zpool || (a.xpool && L.Do % 2 == 0), "tc layer: a z-pooled output needs the x-pooled form, even Do");
+    if (L.fp8_out) {
+      if (a.zpool) return launch_dxf2<true, true, true>(kp, smem, s);
+      return a.xpool ? launch_dxf2<true, true, false>(kp, smem, s) : launch_dxf2<true, false, false>(kp, smem, s);
+    }
+    if (a.zpool) return launch_dxf2<false, true, true>(kp, smem, s);
+    return a.xpool ? launch_dxf2<false, true, false>(kp, smem, s) : launch_dxf2<false, false, false>(kp, smem, s);
   }
   if (L.dxf) {
     TDM_REQUIRE(tc_layer_fits(L), "tc layer: unsupported dx-fused tile");

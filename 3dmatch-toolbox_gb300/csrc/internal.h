@@ -17,11 +17,12 @@ tdm_status launch_conv1(const float* patches, int B, const float* w, const float
 tdm_status launch_conv_f32(const float* in, int B, int D, int C, int ks, const float* w, const float* bias, int K,
                            bool relu, float* out, cudaStream_t s);
 tdm_status launch_pool_f32(const float* in, int B, int D, int C, float* out, cudaStream_t s);
-// x_pooled: the input's x extent is already D/2 (max of x pairs, from conv2's epilogue)
+// x_pooled: the input's x extent is already D/2 (max of x pairs, from conv2's epilogue);
+// z_pooled (with x_pooled): so is its z extent (max of z pairs)
 tdm_status launch_pool_c16_u8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out,
-                              int64_t out_cs, cudaStream_t s, bool x_pooled = false);
+                              int64_t out_cs, cudaStream_t s, bool x_pooled = false, bool z_pooled = false);
 tdm_status launch_pool_c8(const uint8_t* in, int64_t in_cs, int B, int D, int nchunks, uint8_t* out, int64_t out_cs,
-                          cudaStream_t s, bool x_pooled = false);
+                          cudaStream_t s, bool x_pooled = false, bool z_pooled = false);
 
 // ---- conv_tc.cu: tcgen05 implicit-GEMM convolution / GEMM ----
 // Output layouts of the tensor-core epilogue.
@@ -82,12 +83,16 @@ struct TcArgs {
   float in_scale;  // FP8: activation dequantisation scale of the input
   float out_qinv;  // FP8 output: 1/scale used to quantise
   bool xpool = false;  // dx-fused conv2: write the max of each x pair (x extent Do/2)
+  bool zpool = false;  // with xpool, CTA-pair form only: also the max of each z pair (z extent Do/2)
   float* part = nullptr;  // split-K partial sums, [ksplit][rows][cout] FP32
 };
 
 // Rows of slack a chunk-planar input needs after its last row for layer L.
 int64_t tc_tail_rows(const TcLayer& L);
 tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s);
+// Whether launch_tc_layer runs layer L over `rows` input rows in the CTA-pair
+// form (which alone can take the z-pair max, TcArgs::zpool).
+bool tc_pair_form_applies(const TcLayer& L, int64_t rows);
 // conv1 with its im2col operand built in shared memory (L = the conv1 GEMM
 // layer's packed weights and bias); writes conv2's chunk-planar BF16 input.
 tdm_status launch_conv1_tc(const float* patches, int B, const TcLayer& L, uint8_t* out, int64_t out_cs,

@@ -460,6 +460,8 @@ tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, in
       a.out_cs = out_cs;
       // the epilogue takes the pool's x-pair max unless conv2's own response is wanted
       a.xpool = stop != 1 && L.dxf;
+      // the CTA-pair form also takes the z-pair max (z extent 13)
+      a.zpool = a.xpool && tc_pair_form_applies(L, a.rows);
     } else {
       out_cs = P.rows_alloc[l + 1] * 16;
       a.out = dst;
@@ -478,8 +480,8 @@ tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, in
     if (l == 1) {  // pool 26^3 -> 13^3 back into buffer 0 as conv3's input
       int64_t pcs = P.rows_alloc[2] * 16;
       ev = net->begin(9, s);
-      st = fp8 ? launch_pool_c16_u8(dst, out_cs, B, 26, 4, cur, pcs, s, a.xpool)
-               : launch_pool_c8(dst, out_cs, B, 26, 8, cur, pcs, s, a.xpool);
+      st = fp8 ? launch_pool_c16_u8(dst, out_cs, B, 26, 4, cur, pcs, s, a.xpool, a.zpool)
+               : launch_pool_c8(dst, out_cs, B, 26, 8, cur, pcs, s, a.xpool, a.zpool);
       net->end(ev, s);
       if (st) return st;
       if (stop == kPool) {

@@ -145,14 +145,19 @@ __global__ __launch_bounds__(1024) void finalize_kernel(const float* __restrict_
         while (N > (double)tc && tc < iters) {
           int c = counts[tc];
           if (c >= bestscore) {
+            // a tie keeps N: it is a function of the count alone (the FP64
+            // logarithms are the loop's slow part on this GPU)
+            const bool grew = c > bestscore || h < 0;
             bestscore = c;
             h = tc;
-            double w = (double)c / (double)m;
-            double pno = 1.0 - w * w * w;
-            if (pno < eps) pno = eps;
-            if (pno > 1.0 - eps) pno = 1.0 - eps;
-            N = log(1.0 - p) / log(pno);
-            if (N < 10.0) N = 10.0;
+            if (grew) {
+              double w = (double)c / (double)m;
+              double pno = 1.0 - w * w * w;
+              if (pno < eps) pno = eps;
+              if (pno > 1.0 - eps) pno = 1.0 - eps;
+              N = log(1.0 - p) / log(pno);
+              if (N < 10.0) N = 10.0;
+            }
           }
           tc++;
           if (tc > max_trials) break;

@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--descriptors", action="store_true", help="descriptor throughput workload (5000 patches)")
     ap.add_argument("--batch", action="store_true", help="batched uneven fragments workload (64 fragments)")
     ap.add_argument("--batch-fragments", type=int, default=64)
+    ap.add_argument("--net-chunk", type=int, default=0,
+                    help="batched form: patches per net launch (0 = the library default, 2,048)")
     ap.add_argument("--registration", action="store_true",
                     help="registration benchmark scored in the reference's metric (synthetic scene)")
     ap.add_argument("--reg-views", type=int, default=8)
@@ -818,6 +820,8 @@ def run_batch(args, rank, world, local):
             net.calibrate(tune[:256].contiguous())
         if prec != "fp32":
             tiles = net.autotune(tune, reps=2)
+        if args.net_chunk > 0:
+            net.set_max_batch(args.net_chunk)
         batch = tdm.Batch(net, max_fragments=F, max_points=pts.shape[0], max_keypoints=K,
                           max_voxels=3_000_000_000, use_graph=True)
         steps = args.steps if prec != "fp32" else 1
