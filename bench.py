@@ -34,6 +34,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONV2_FLOP_PER_PATCH = 2.0 * 26 ** 3 * 64 * (27 * 64)  # useful FLOPs of conv2 (algorithmic)
+# MMA work the CTA-pair conv2 issues per patch: 78 tiles (3 blocks of 252 plane rows x 26 z)
+# x 36 MMAs of 256 x 192 x 16 (1.14x the useful work: rows with y = 26, dx taps of x >= 26)
+CONV2_MMA_FLOP_PER_PATCH = 78 * 36 * 2 * 256 * 192 * 16
+# the MMA rate measured by the tcgen05 probe: 4,096 MAC/clk/SM
+MMA_MAC_PER_CLK_SM = 4096
 NET_FLOP_PER_PATCH = 6.452e9
 
 
@@ -467,11 +472,16 @@ def run_ours(args, rank, world, local):
         # burst peak: conv2 runs inside a ~14 ms step at full clocks, not a
         # seconds-long loop under the power cap
         peak = peaks["bf16_tflops"] if prec == "bf16" else None
-        roof = {"kernel": "tc_conv_dxf2_kernel<bf16,x-pooled> (conv2 on CTA pairs, %d patches per launch)" % (2 * k),
+        roof = {"kernel": "tc_conv_dxf2_kernel<bf16,x-pooled,z-pooled> (conv2 on CTA pairs, %d patches per launch)" % (2 * k),
                 "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if peak else None, "peak_source": peak_kind + " bf16 burst",
                 "traffic": profile_traffic("conv2_pair_bf16"),
-                "ms_per_launch": conv2_ms / conv2_n, "share_of_step": (conv2_ms / args.steps) / ms_step}
+                "ms_per_launch": conv2_ms / conv2_n, "share_of_step": (conv2_ms / args.steps) / ms_step,
+                "note": "achieved counts useful FLOPs (valid outputs); the kernel issues %.2fx that in MMAs "
+                        "(%.0f TFLOP/s of MMA work), and the measured burst peak is a cuBLAS GEMM, below the "
+                        "probe's %d MAC/clk/SM" % (CONV2_MMA_FLOP_PER_PATCH / CONV2_FLOP_PER_PATCH,
+                                                  achieved * CONV2_MMA_FLOP_PER_PATCH / CONV2_FLOP_PER_PATCH,
+                                                  MMA_MAC_PER_CLK_SM)}
     layer_ms = {name: round(v[0] / max(1, v[1]), 4) for name, v in lt.items() if v[1]}
     out = None
     if rank == 0:
