@@ -667,6 +667,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
     // ---------------- epilogue (warps 2-5 and 10-13: TMEM lane quarter warp % 4,
     // column half eh) ----------------
     const int q = warp & 3, eh = warp >= 10 ? 1 : 0;
+    const bool rows32 = p.rows <= INT32_MAX;
     uint32_t j = 0;
     for (int64_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
       const int64_t m0 = (t / p.ntiles) * MCTA;
@@ -721,7 +722,7 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
             bool valid = row < p.rows;
             int64_t pos;
             if (XRUN) {
-              const int64_t yz = row / Dx;
+              const int64_t yz = row_div(row, Dx, rows32);
               const int x = (int)(row - yz * Dx);
               valid = valid && x < p.Do;
               pos = yz * p.Do + x;  // ((b*Do + z)*Do + y)*Do + x
@@ -743,13 +744,13 @@ __global__ void __launch_bounds__(kGThreads, 1) tc_conv_gather_kernel(const KPar
         int64_t b, pos;  // patch, output position (row of the next layer's grid)
         int tap;         // output position within the patch
         if (XRUN) {      // rows (b, z, y, x < D): outputs where x < Do
-          const int64_t yz = row / Dx;
+          const int64_t yz = row_div(row, Dx, rows32);
           const int x = (int)(row - yz * Dx);
           valid = valid && x < p.Do;
-          b = yz / Do2;
+          b = row_div(yz, Do2, rows32);
           tap = (int)(yz - b * Do2) * p.Do + x;
         } else {
-          b = row / Do3;
+          b = row_div(row, Do3, rows32);
           tap = (int)(row - b * Do3);
         }
         pos = b * Do3 + tap;
