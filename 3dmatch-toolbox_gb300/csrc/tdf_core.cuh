@@ -6,6 +6,9 @@
 
 #include <cmath>
 #include <cstdint>
+#ifdef __CUDACC__
+#include <cuda_fp16.h>
+#endif
 
 #include "tdm.h"
 
@@ -51,6 +54,41 @@ __device__ __forceinline__ int voxel_coord(float p, float o, float vs) {
 // 200, "none" is 0xFF, and sums saturate at 0xFF (__vaddus4), which maps every
 // distance above R^2 to the same value 0 as the reference.
 __host__ __device__ inline int64_t occ_pitch(int dx) { return ((int64_t)dx + 3) & ~(int64_t)3; }
+
+// Min-plus on packed squared distances.  The saturating byte form
+//   best = min_k min(255, g_k + d_k^2)
+// is computed as min(255, min_k (g_k + d_k^2)) in half2 lanes holding 1024 + g
+// (bytes placed under the FP16 exponent of 1024, whose ulp is 1): every value
+// stays an integer below 2048, exact in FP16, so the bytes are the byte form's,
+// with two voxels per HADD2/HMNMX2 instead of the byte-SIMD emulation.
+__device__ __forceinline__ void bytes_to_h2(uint32_t w, uint32_t& lo, uint32_t& hi) {
+  lo = __byte_perm(w, 0x64646464u, 0x4140);  // (1024 + b0, 1024 + b1)
+  hi = __byte_perm(w, 0x64646464u, 0x4342);  // (1024 + b2, 1024 + b3)
+}
+__device__ __forceinline__ uint32_t h2_add(uint32_t a, uint32_t b) {
+  __half2 r = __hadd2(*reinterpret_cast<const __half2*>(&a), *reinterpret_cast<const __half2*>(&b));
+  return *reinterpret_cast<uint32_t*>(&r);
+}
+__device__ __forceinline__ uint32_t h2_min(uint32_t a, uint32_t b) {
+  __half2 r = __hmin2(*reinterpret_cast<const __half2*>(&a), *reinterpret_cast<const __half2*>(&b));
+  return *reinterpret_cast<uint32_t*>(&r);
+}
+// FP16 bits of an integer 0 <= n < 2048 (exact: 11 significant bits)
+__host__ __device__ constexpr uint32_t fp16_bits_of_int(int n) {
+  int e = 0;
+  while (e < 10 && (n >> (e + 1)) != 0) ++e;
+  return n == 0 ? 0u : (uint32_t)(((e + 15) << 10) | ((n - (1 << e)) << (10 - e)));
+}
+static_assert(fp16_bits_of_int(1024) == 0x6400u && fp16_bits_of_int(25) == 0x4E40u, "FP16 integer encoding");
+// the squared offset k^2 in both lanes (k^2 <= 100)
+__device__ __forceinline__ constexpr uint32_t h2_sq(int k) { return fp16_bits_of_int(k * k) * 0x10001u; }
+// min(255, value - 1024) of both lanes of lo and hi, packed back into 4 bytes
+__device__ __forceinline__ uint32_t h2_to_bytes(uint32_t lo, uint32_t hi) {
+  constexpr uint32_t kCap = 0x64FF64FFu;  // (1024 + 255) in both lanes
+  lo = h2_min(lo, kCap);
+  hi = h2_min(hi, kCap);
+  return __byte_perm(lo, hi, 0x6420);
+}
 
 constexpr int PB_TX = 128, PB_TY = 16;  // in-plane tile: 128 x positions, 16 rows
 constexpr int PB_HALO = 12;             // staged bytes left of the tile (>= R, multiple of 4)
@@ -138,9 +176,18 @@ __device__ __forceinline__ void plane_tile(const uint8_t* __restrict__ occ, int 
     for (int d = -R; d <= R; ++d) all &= sm.g1[ly + R + d][g];
     uint32_t best = 0xFFFFFFFFu;
     if (all != 0xFFFFFFFFu) {
+      uint32_t bl, bh;
+      bytes_to_h2(sm.g1[ly][g], bl, bh);
+      bl = h2_add(bl, h2_sq(R));
+      bh = h2_add(bh, h2_sq(R));
 #pragma unroll
-      for (int d = -R; d <= R; ++d)
-        best = __vminu4(best, __vaddus4(sm.g1[ly + R + d][g], (uint32_t)(d * d) * 0x01010101u));
+      for (int d = -R + 1; d <= R; ++d) {
+        uint32_t l, h;
+        bytes_to_h2(sm.g1[ly + R + d][g], l, h);
+        bl = h2_min(bl, h2_add(l, h2_sq(d)));
+        bh = h2_min(bh, h2_add(h, h2_sq(d)));
+      }
+      best = h2_to_bytes(bl, bh);
     }
     *reinterpret_cast<uint32_t*>(g2 + zbase + (int64_t)(y0 + ly) * X + x0 + 4 * g) = best;
   }
@@ -174,21 +221,26 @@ __device__ __forceinline__ void z_column(const uint8_t* __restrict__ g2, int dx,
   auto word = [&](int zz) -> uint32_t {
     return (live && zz >= 0 && zz < dz) ? __ldg(reinterpret_cast<const uint32_t*>(col + zz * pz)) : 0xFFFFFFFFu;
   };
-  uint32_t ring[2 * R + 1];
+  // the window's words as half2 pairs of 1024 + byte (see bytes_to_h2)
+  uint32_t rlo[2 * R + 1], rhi[2 * R + 1];
 #pragma unroll
-  for (int k = 0; k < 2 * R + 1; ++k) ring[k] = word(z0 - R + k);
+  for (int k = 0; k < 2 * R + 1; ++k) bytes_to_h2(word(z0 - R + k), rlo[k], rhi[k]);
   const int n = min(128, dx - xseg);
   for (int z = z0; z < z1; ++z) {
-    // the byte-SIMD min-plus is many ALU instructions per word: when every byte
-    // of the window is "none" (0xFF, most of a grid) its result is 0xFF anyway
-    uint32_t all = ring[0];
+    // when every byte of the window is "none" (0xFF, most of a grid) the
+    // min-plus gives 0xFF anyway: (1024 + 255) in every lane
+    uint32_t all = rlo[0] & rhi[0];
 #pragma unroll
-    for (int k = 1; k < 2 * R + 1; ++k) all &= ring[k];
+    for (int k = 1; k < 2 * R + 1; ++k) all &= rlo[k] & rhi[k];
     uint32_t best = 0xFFFFFFFFu;
-    if (all != 0xFFFFFFFFu) {
+    if (all != 0x64FF64FFu) {
+      uint32_t bl = h2_add(rlo[0], h2_sq(R)), bh = h2_add(rhi[0], h2_sq(R));
 #pragma unroll
-      for (int k = 0; k < 2 * R + 1; ++k)
-        best = __vminu4(best, __vaddus4(ring[k], (uint32_t)((k - R) * (k - R)) * 0x01010101u));
+      for (int k = 1; k < 2 * R + 1; ++k) {
+        bl = h2_min(bl, h2_add(rlo[k], h2_sq(k - R)));
+        bh = h2_min(bh, h2_add(rhi[k], h2_sq(k - R)));
+      }
+      best = h2_to_bytes(bl, bh);
     }
     float* out = tdf + ((int64_t)z * dy + y) * dx + xseg;
     if (__all_sync(0xffffffffu, best == 0xFFFFFFFFu)) {
@@ -207,8 +259,11 @@ __device__ __forceinline__ void z_column(const uint8_t* __restrict__ g2, int dx,
       __syncwarp();
     }
 #pragma unroll
-    for (int k = 0; k < 2 * R; ++k) ring[k] = ring[k + 1];
-    ring[2 * R] = word(z + R + 1);
+    for (int k = 0; k < 2 * R; ++k) {
+      rlo[k] = rlo[k + 1];
+      rhi[k] = rhi[k + 1];
+    }
+    bytes_to_h2(word(z + R + 1), rlo[2 * R], rhi[2 * R]);
   }
 }
 
