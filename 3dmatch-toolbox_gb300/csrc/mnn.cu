@@ -188,46 +188,67 @@ __global__ void nn_rows_kernel(const float* __restrict__ dot, int64_t ld, int nq
 }
 
 // Column scan over `dot` [nr][ld]: query j is a column, candidates are the
-// rows i.  A block owns 32 consecutive columns (lane = column) and its 16
-// warps split the rows, so each row read is one coalesced 128-byte line; the
-// per-warp lists are merged in shared memory.  Query index g = goff + j.
-constexpr int COL_WARPS = 16;
+// rows i.  A block owns 8 consecutive columns: lane = (row group lane / 8,
+// column lane % 8), so one warp load reads 4 rows x 32 bytes (one sector
+// each), and the 16 warps split the rows; 8 columns per block give 1,000
+// columns 125 blocks.  A warp's four row-group lists are merged with
+// shuffles, the warps' lists in shared memory.  The top 4 of a set under the
+// (distance, index) order does not depend on the merge order.  Query index
+// g = goff + j.
+constexpr int COL_WARPS = 16, COL_COLS = 8, COL_GROUPS = 32 / COL_COLS;
 
 __global__ void __launch_bounds__(COL_WARPS * 32)
 nn_cols_kernel(const float* __restrict__ dot, int64_t ld, int nq, int nr, const float* __restrict__ qn,
                const float* __restrict__ rn, const float* __restrict__ rn_max_ptr, int dim, int exact, int goff,
                int32_t* __restrict__ cand, int32_t* __restrict__ full, int32_t* __restrict__ n_full) {
-  __shared__ float s_d[COL_WARPS][TOPK][32];
-  __shared__ int s_j[COL_WARPS][TOPK][32];
+  __shared__ float s_d[COL_WARPS][TOPK][COL_COLS];
+  __shared__ int s_j[COL_WARPS][TOPK][COL_COLS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int j = blockIdx.x * 32 + lane;
+  const int col = lane % COL_COLS, grp = lane / COL_COLS;
+  const int j = blockIdx.x * COL_COLS + col;
   const bool live = j < nq;
   Cand c;
   cand_init(c);
   if (live) {
+    constexpr int STEP = COL_WARPS * COL_GROUPS;  // rows per pass of the block
     const float qj = qn[j];
-    int i = w;
-    for (; i + 3 * COL_WARPS < nr; i += 4 * COL_WARPS) {  // four rows in flight
+    int i = w * COL_GROUPS + grp;
+    for (; i + 3 * STEP < nr; i += 4 * STEP) {  // four rows in flight
       float v[4], n[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        v[u] = __ldg(dot + (int64_t)(i + u * COL_WARPS) * ld + j);
-        n[u] = __ldg(rn + i + u * COL_WARPS);
+        v[u] = __ldg(dot + (int64_t)(i + u * STEP) * ld + j);
+        n[u] = __ldg(rn + i + u * STEP);
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) cand_push(c, qj + n[u] - 2.0f * v[u], i + u * COL_WARPS);
+      for (int u = 0; u < 4; ++u) cand_push(c, qj + n[u] - 2.0f * v[u], i + u * STEP);
     }
-    for (; i < nr; i += COL_WARPS) cand_push(c, qj + __ldg(rn + i) - 2.0f * __ldg(dot + (int64_t)i * ld + j), i);
+    for (; i < nr; i += STEP) cand_push(c, qj + __ldg(rn + i) - 2.0f * __ldg(dot + (int64_t)i * ld + j), i);
   }
+  // lanes col, col + 8, col + 16, col + 24 scanned disjoint rows of one column
 #pragma unroll
-  for (int t = 0; t < TOPK; ++t) { s_d[w][t][lane] = c.d[t]; s_j[w][t][lane] = c.j[t]; }
+  for (int o = COL_COLS; o < 32; o <<= 1) {
+    float od[TOPK];
+    int oj[TOPK];
+#pragma unroll
+    for (int t = 0; t < TOPK; ++t) {
+      od[t] = __shfl_xor_sync(0xffffffffu, c.d[t], o);
+      oj[t] = __shfl_xor_sync(0xffffffffu, c.j[t], o);
+    }
+#pragma unroll
+    for (int t = 0; t < TOPK; ++t) cand_push(c, od[t], oj[t]);
+  }
+  if (grp == 0) {
+#pragma unroll
+    for (int t = 0; t < TOPK; ++t) { s_d[w][t][col] = c.d[t]; s_j[w][t][col] = c.j[t]; }
+  }
   __syncthreads();
-  if (w == 0 && live) {
+  if (w == 0 && grp == 0 && live) {
     Cand m;
     cand_init(m);
     for (int v = 0; v < COL_WARPS; ++v)
 #pragma unroll
-      for (int t = 0; t < TOPK; ++t) cand_push(m, s_d[v][t][lane], s_j[v][t][lane]);
+      for (int t = 0; t < TOPK; ++t) cand_push(m, s_d[v][t][col], s_j[v][t][col]);
     put_candidates(m, qn[j], *rn_max_ptr, nr, dim, exact, goff + j, cand, full, n_full);
   }
 }
@@ -281,6 +302,19 @@ __global__ void rescore_kernel(const float* __restrict__ a, const float* __restr
 // the 32 slices; the minimum (ties -> lower index) wins.  The sums differ from
 // the oracle's k-ordered ones only in the last bits of double, far below the
 // BF16 candidates' own error; the FP32 form keeps rescore_kernel.
+//
+// The same sums are first taken in FP32.  Every term is non-negative, so an
+// FP32 sum lies within REL * sum + ABS of the exact one: a lane's slice and
+// the tree round at most dim/32 + 5 times, each square and difference adds
+// two roundings (2^-24 each, ~1.4e-6 for dim 512; REL = 4e-6 leaves a margin
+// of ~3), and squares below the normal range lose at most 2^-150 each (ABS).
+// When the best candidate's interval lies below every other candidate's, the
+// exact sums and the FP64 ones (whose own error is ~1e-15 relative) pick that
+// candidate too, and the FP64 pass is skipped; otherwise (near-ties, NaN,
+// overflow) the query takes the FP64 pass.  So the chosen index is the FP64
+// pass's in every case.  The FP32 sums and the decision are identical in all
+// lanes (xor butterflies: each add's operands are swapped, not regrouped), so
+// the branch is warp-uniform.
 __global__ void __launch_bounds__(256) rescore_warp_kernel(const float* __restrict__ a, const float* __restrict__ b,
                                                            int na, int nb, int dim, const int32_t* __restrict__ cand,
                                                            int32_t* __restrict__ nn_ab, int32_t* __restrict__ nn_ba) {
@@ -297,6 +331,43 @@ __global__ void __launch_bounds__(256) rescore_warp_kernel(const float* __restri
     const int j = cand[TOPK * g + c];
     cj[c] = (j >= 0 && j < Q.nr) ? j : -1;
     part[c] = 0.0;
+  }
+  {
+    float pf[TOPK];
+#pragma unroll
+    for (int c = 0; c < TOPK; ++c) pf[c] = 0.0f;
+    for (int k = k0; k < k0 + per; k += 2) {
+      const float2 x = *reinterpret_cast<const float2*>(Q.q + k);
+#pragma unroll
+      for (int c = 0; c < TOPK; ++c) {
+        if (cj[c] < 0) continue;
+        const float2 y = *reinterpret_cast<const float2*>(Q.r + (int64_t)cj[c] * dim + k);
+        float d = x.x - y.x;
+        pf[c] = fmaf(d, d, pf[c]);
+        d = x.y - y.y;
+        pf[c] = fmaf(d, d, pf[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < TOPK; ++c)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) pf[c] += __shfl_xor_sync(0xffffffffu, pf[c], o);
+    constexpr float REL = 4e-6f, ABS = 1e-40f;
+    int bc = -1;
+#pragma unroll
+    for (int c = 0; c < TOPK; ++c)
+      if (cj[c] >= 0 && (bc < 0 || pf[c] < pf[bc])) bc = c;
+    bool decided = bc >= 0 && pf[bc] == pf[bc];
+    if (decided) {
+      const float hi = pf[bc] + (REL * pf[bc] + ABS);
+#pragma unroll
+      for (int c = 0; c < TOPK; ++c)
+        if (c != bc && cj[c] >= 0 && !(pf[c] - (REL * pf[c] + ABS) > hi)) decided = false;
+    }
+    if (decided) {
+      if (lane == 0) *Q.out = cj[bc];
+      return;
+    }
   }
   for (int k = k0; k < k0 + per; k += 2) {
     const float2 x = *reinterpret_cast<const float2*>(Q.q + k);
@@ -396,7 +467,11 @@ __global__ void mutual_kernel(const int32_t* __restrict__ nn_ab, const int32_t* 
   if (threadIdx.x == 0) *n_pairs = s_base;
 }
 
-__global__ void max_kernel(const float* __restrict__ x, int n, float* __restrict__ out) {
+// Block 0: max of x0[0..n0), block 1: max of x1[0..n1) (into out[0], out[1]).
+__global__ void max2_kernel(const float* __restrict__ x0, int n0, const float* __restrict__ x1, int n1,
+                            float* __restrict__ out) {
+  const float* x = blockIdx.x == 0 ? x0 : x1;
+  const int n = blockIdx.x == 0 ? n0 : n1;
   float m = 0.0f;
   for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, x[i]);
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -405,7 +480,7 @@ __global__ void max_kernel(const float* __restrict__ x, int n, float* __restrict
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, s[w]);
-    *out = m;
+    out[blockIdx.x] = m;
   }
 }
 
@@ -462,9 +537,8 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
   float* maxes = reinterpret_cast<float*>(w + L.maxes);
   sqnorm_kernel<<<(na + 7) / 8, 256, 0, s>>>(da, na, dim, an);
   sqnorm_kernel<<<(nb + 7) / 8, 256, 0, s>>>(db, nb, dim, bn);
-  max_kernel<<<1, 1024, 0, s>>>(an, na, maxes);
-  max_kernel<<<1, 1024, 0, s>>>(bn, nb, maxes + 1);
-  note_launches(3);
+  max2_kernel<<<2, 1024, 0, s>>>(an, na, bn, nb, maxes);
+  note_launches(2);
   TDM_CHECK_LAUNCH("mnn norms");
   float* zeros = reinterpret_cast<float*>(w + L.zeros);
   int32_t* n_full = reinterpret_cast<int32_t*>(zeros + L.nbp);
@@ -510,9 +584,9 @@ extern "C" tdm_status tdm_match_mnn(const float* da, int32_t na, const float* db
     if (st) return st;
   }
   const int exact = prec == TDM_FP32 ? 1 : 0;
-  // candidates: rows a -> b (warp per row), columns b -> a (32 columns per block)
+  // candidates: rows a -> b (warp per row), columns b -> a (8 columns per block)
   nn_rows_kernel<<<(na + 7) / 8, 256, 0, s>>>(dot, L.nbp, na, nb, an, bn, maxes + 1, dim, exact, cand, full, n_full);
-  nn_cols_kernel<<<(nb + 31) / 32, COL_WARPS * 32, 0, s>>>(dot, L.nbp, nb, na, bn, an, maxes, dim, exact, na, cand,
+  nn_cols_kernel<<<(nb + COL_COLS - 1) / COL_COLS, COL_WARPS * 32, 0, s>>>(dot, L.nbp, nb, na, bn, an, maxes, dim, exact, na, cand,
                                                           full, n_full);
   const int64_t lanes = (int64_t)(na + nb) * TOPK;
   if (exact) {

@@ -45,23 +45,148 @@ __device__ void sample3(uint64_t seed, uint32_t h, int m, int s[3]) {
   s[0] = (int)i0; s[1] = (int)i1; s[2] = (int)i2;
 }
 
-// Kabsch on the listed correspondences (idx == nullptr: 0..n-1).
-__device__ bool kabsch(const float* x, const float* y, const int* idx, int n, double R[9], double t[3]) {
-  double cx[3] = {0, 0, 0}, cy[3] = {0, 0, 0};
-  for (int i = 0; i < n; ++i) {
-    int k = idx ? idx[i] : i;
-    for (int a = 0; a < 3; ++a) { cx[a] += (double)x[3 * k + a]; cy[a] += (double)y[3 * k + a]; }
+// FP64 Kabsch refit on the listed correspondences, run by one whole warp.
+// The one-thread form is: centroids cx, cy summed in list order and divided
+// by n; H[a][b] = sum over the list of (y[a] - cy[a]) (x[b] - cx[b]); then
+// kabsch_from_h (kabsch.cuh; the host ICP and the oracle use the same steps).
+// GB300 issues an FP64 warp instruction at a fixed cost whatever the number of
+// active lanes, so a one-thread refit pays for 32 lanes per operation; here
+// values that do not depend on one another (the six centroid sums, the nine
+// covariance sums, the rows of each Jacobi rotation, R and t) are computed by
+// different lanes with one instruction stream.  Each value goes through the
+// same operations in the same order as in the one-thread form (the
+// translation unit is built without contraction), so every bit is the same.
+// Every lane returns the fit.
+__device__ __forceinline__ double pick3(int i, double a0, double a1, double a2) {
+  return i == 0 ? a0 : (i == 1 ? a1 : a2);
+}
+
+__device__ void jacobi3_warp(double A[3][3], double V[3][3], double ev[3]) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int k = lane < 3 ? lane : (lane < 6 ? lane - 3 : 0);  // row of A (lanes 0-2) or of V (lanes 3-5)
+  const bool vrow = lane >= 3 && lane < 6;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 24; ++sweep) {
+    double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+    double scale = fabs(A[0][0]) + fabs(A[1][1]) + fabs(A[2][2]);
+    if (off <= 1e-300 || off <= 1e-18 * scale) break;
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int q = p + 1; q < 3; ++q) {
+        double apq = A[p][q];
+        if (apq == 0.0) continue;  // A is the same in every lane: a uniform branch
+        double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+        double t = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
+        if (theta < 0.0) t = -t;
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        // columns p, q of row k of A (lanes 0-2) and of V (lanes 3-5)
+        {
+          const double u = vrow ? pick3(k, V[0][p], V[1][p], V[2][p]) : pick3(k, A[0][p], A[1][p], A[2][p]);
+          const double v = vrow ? pick3(k, V[0][q], V[1][q], V[2][q]) : pick3(k, A[0][q], A[1][q], A[2][q]);
+          const double np = c * u - s * v, nq = s * u + c * v;
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            A[r][p] = __shfl_sync(full, np, r);
+            A[r][q] = __shfl_sync(full, nq, r);
+            V[r][p] = __shfl_sync(full, np, 3 + r);
+            V[r][q] = __shfl_sync(full, nq, 3 + r);
+          }
+        }
+        // rows p, q of column k of A (lanes 0-2), from the updated columns
+        {
+          const double u = pick3(k, A[p][0], A[p][1], A[p][2]);
+          const double v = pick3(k, A[q][0], A[q][1], A[q][2]);
+          const double np = c * u - s * v, nq = s * u + c * v;
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            A[p][r] = __shfl_sync(full, np, r);
+            A[q][r] = __shfl_sync(full, nq, r);
+          }
+        }
+      }
   }
-  for (int a = 0; a < 3; ++a) { cx[a] /= (double)n; cy[a] /= (double)n; }
-  double H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  for (int i = 0; i < n; ++i) {
-    int k = idx ? idx[i] : i;
-    double dx[3], dy[3];
-    for (int a = 0; a < 3; ++a) { dx[a] = (double)x[3 * k + a] - cx[a]; dy[a] = (double)y[3 * k + a] - cy[a]; }
-    for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b) H[a][b] += dy[a] * dx[b];
+  for (int i = 0; i < 3; ++i) ev[i] = A[i][i];
+}
+
+__device__ bool kabsch_warp(const float* x, const float* y, const int* idx, int n, double R[9], double t[3]) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  // centroids: lanes 0-2 sum x[.][lane], lanes 3-5 sum y[.][lane - 3], in list order
+  const float* src = lane < 3 ? x : y;
+  const int comp = lane < 3 ? lane : (lane < 6 ? lane - 3 : 0);
+  double acc = 0.0;
+  for (int i = 0; i < n; ++i) acc += (double)src[3 * idx[i] + comp];
+  acc /= (double)n;
+  double cx[3], cy[3];
+  for (int a = 0; a < 3; ++a) {
+    cx[a] = __shfl_sync(full, acc, a);
+    cy[a] = __shfl_sync(full, acc, 3 + a);
   }
-  return kabsch_from_h(H, cx, cy, R, t);
+  // covariance H[a][b] = sum dy[a] dx[b]: lane 3a + b, in list order
+  const int ha = lane < 9 ? lane / 3 : 0, hb = lane < 9 ? lane % 3 : 0;
+  const double cya = pick3(ha, cy[0], cy[1], cy[2]), cxb = pick3(hb, cx[0], cx[1], cx[2]);
+  double hs = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const int k = idx[i];
+    const double dy = (double)y[3 * k + ha] - cya;
+    const double dx = (double)x[3 * k + hb] - cxb;
+    hs += dy * dx;
+  }
+  double H[3][3];
+  for (int r = 0; r < 9; ++r) H[r / 3][r % 3] = __shfl_sync(full, hs, r);
+  // M = H^T H: lane 3i + j
+  double ms = 0.0;
+  for (int kk = 0; kk < 3; ++kk)
+    ms += pick3(ha, H[kk][0], H[kk][1], H[kk][2]) * pick3(hb, H[kk][0], H[kk][1], H[kk][2]);
+  double M[3][3], V[3][3], ev[3];
+  for (int r = 0; r < 9; ++r) M[r / 3][r % 3] = __shfl_sync(full, ms, r);
+  jacobi3_warp(M, V, ev);
+  // the rest as in kabsch_from_h, the same in every lane
+  int o[3] = {0, 1, 2};
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2 - i; ++j)
+      if (ev[o[j]] < ev[o[j + 1]]) { int tmp = o[j]; o[j] = o[j + 1]; o[j + 1] = tmp; }
+  double v[3][3], u[3][3];
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) v[c][r] = V[r][o[c]];
+  v[2][0] = v[0][1] * v[1][2] - v[0][2] * v[1][1];
+  v[2][1] = v[0][2] * v[1][0] - v[0][0] * v[1][2];
+  v[2][2] = v[0][0] * v[1][1] - v[0][1] * v[1][0];
+  for (int c = 0; c < 2; ++c) {
+    double hv[3], nn = 0.0;
+    for (int r = 0; r < 3; ++r) {
+      hv[r] = H[r][0] * v[c][0] + H[r][1] * v[c][1] + H[r][2] * v[c][2];
+      nn += hv[r] * hv[r];
+    }
+    nn = sqrt(nn);
+    if (!(nn > 1e-300)) return false;
+    for (int r = 0; r < 3; ++r) u[c][r] = hv[r] / nn;
+  }
+  {
+    double d = u[0][0] * u[1][0] + u[0][1] * u[1][1] + u[0][2] * u[1][2], nn = 0.0;
+    for (int r = 0; r < 3; ++r) { u[1][r] = u[1][r] - d * u[0][r]; nn += u[1][r] * u[1][r]; }
+    nn = sqrt(nn);
+    if (!(nn > 1e-300)) return false;
+    for (int r = 0; r < 3; ++r) u[1][r] = u[1][r] / nn;
+  }
+  u[2][0] = u[0][1] * u[1][2] - u[0][2] * u[1][1];
+  u[2][1] = u[0][2] * u[1][0] - u[0][0] * u[1][2];
+  u[2][2] = u[0][0] * u[1][1] - u[0][1] * u[1][0];
+  // R[3i + j]: lane 3i + j
+  const double rr = pick3(ha, v[0][0], v[0][1], v[0][2]) * pick3(hb, u[0][0], u[0][1], u[0][2]) +
+                    pick3(ha, v[1][0], v[1][1], v[1][2]) * pick3(hb, u[1][0], u[1][1], u[1][2]) +
+                    pick3(ha, v[2][0], v[2][1], v[2][2]) * pick3(hb, u[2][0], u[2][1], u[2][2]);
+  for (int r = 0; r < 9; ++r) R[r] = __shfl_sync(full, rr, r);
+  // t[i]: lane i
+  const int ti = lane < 3 ? lane : 0;
+  const double tt = pick3(ti, cx[0], cx[1], cx[2]) -
+                    (pick3(ti, R[0], R[3], R[6]) * cy[0] + pick3(ti, R[1], R[4], R[7]) * cy[1] +
+                     pick3(ti, R[2], R[5], R[8]) * cy[2]);
+  for (int r = 0; r < 3; ++r) t[r] = __shfl_sync(full, tt, r);
+  return true;
 }
 
 __device__ __forceinline__ bool is_inlier(const float* xi, const float* yi, const float Rf[9], const float tf[3],
@@ -100,24 +225,41 @@ __global__ __launch_bounds__(256) void trials_kernel(const float* __restrict__ x
   }
   __syncthreads();
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
-  if (h >= iters) return;
-  int c = 0;
-  if (m >= 3) {
-    const float* xs = staged ? sp : x;
-    const float* ys = staged ? sp + 3 * smem_pts : y;
-    float Rf[9], tf[3];
-    if (trial_model(xs, ys, m, seed, (uint32_t)h, Rf, tf)) {
-      // kept for the winner: the finalize step reads it instead of refitting
-      float4* mo = reinterpret_cast<float4*>(models + 12 * (int64_t)h);
-      mo[0] = make_float4(Rf[0], Rf[1], Rf[2], Rf[3]);
-      mo[1] = make_float4(Rf[4], Rf[5], Rf[6], Rf[7]);
-      mo[2] = make_float4(Rf[8], tf[0], tf[1], tf[2]);
-      const float thr2 = thr * thr;
-      for (int i = 0; i < m; ++i) c += is_inlier(xs + 3 * i, ys + 3 * i, Rf, tf, thr2) ? 1 : 0;
+  // (count, trial) key of this thread's trial; threads past the last trial
+  // hold 0, which no trial's key is below
+  unsigned long long key = 0;
+  if (h < iters) {
+    int c = 0;
+    if (m >= 3) {
+      const float* xs = staged ? sp : x;
+      const float* ys = staged ? sp + 3 * smem_pts : y;
+      float Rf[9], tf[3];
+      if (trial_model(xs, ys, m, seed, (uint32_t)h, Rf, tf)) {
+        // kept for the winner: the finalize step reads it instead of refitting
+        float4* mo = reinterpret_cast<float4*>(models + 12 * (int64_t)h);
+        mo[0] = make_float4(Rf[0], Rf[1], Rf[2], Rf[3]);
+        mo[1] = make_float4(Rf[4], Rf[5], Rf[6], Rf[7]);
+        mo[2] = make_float4(Rf[8], tf[0], tf[1], tf[2]);
+        const float thr2 = thr * thr;
+        for (int i = 0; i < m; ++i) c += is_inlier(xs + 3 * i, ys + 3 * i, Rf, tf, thr2) ? 1 : 0;
+      }
     }
+    counts[h] = c;
+    key = ((unsigned long long)(uint32_t)c << 32) | (unsigned long long)(uint32_t)h;
   }
-  counts[h] = c;
-  atomicMax(best, ((unsigned long long)(uint32_t)c << 32) | (unsigned long long)(uint32_t)h);
+  // the block's largest key takes one atomic (100k same-word atomics would
+  // queue at one L2 slice); the max is order-free, so the winner is unchanged
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, key, o);
+    key = other > key ? other : key;
+  }
+  __shared__ unsigned long long s_key[8];
+  if ((threadIdx.x & 31) == 0) s_key[threadIdx.x >> 5] = key;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) key = s_key[w] > key ? s_key[w] : key;
+    atomicMax(best, key);
+  }
 }
 
 // Winner, ordered inlier list and FP64 refit (one block).
@@ -200,10 +342,11 @@ __global__ __launch_bounds__(1024) void finalize_kernel(const float* __restrict_
       __syncthreads();
     }
   }
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {  // warp 0: the refit (s_ok and s_base are block-uniform)
     int n = s_ok ? s_base : 0;
     double R[9], t[3];
-    bool fit = n >= 3 && kabsch(x, y, inliers, n, R, t);
+    bool fit = n >= 3 && kabsch_warp(x, y, inliers, n, R, t);
+    if (threadIdx.x != 0) return;
     for (int i = 0; i < 3; ++i) {
       for (int j = 0; j < 3; ++j) rt[4 * i + j] = fit ? R[3 * i + j] : (i == j ? 1.0 : 0.0);
       rt[4 * i + 3] = fit ? t[i] : 0.0;

@@ -124,6 +124,19 @@ def test_ransac_identical_to_oracle(tdm, oracle, cuda, m, iters):
     tdm.device_status()
 
 
+@pytest.mark.parametrize("m,frac,noise", [(60, 0.3, 0.01), (500, 0.9, 0.005), (4000, 0.95, 0.01),
+                                           (300, 0.5, 0.0)])
+def test_ransac_refit_bits_equal_oracle(tdm, oracle, cuda, m, frac, noise):
+    """The FP64 refit (split over a warp's lanes on the device) gives the
+    oracle's one-thread Kabsch bit for bit, from 18 to 3,800 inliers."""
+    rng = np.random.default_rng(100 + m)
+    x, y, _, _ = _correspondences(rng, m, frac, noise)
+    rt, inl, info = _ransac_gpu(tdm, cuda, x, y, m, 4000, seed=77)
+    ref = oracle.ransac(x, y, seed=77, iters=4000, thr=0.05)
+    assert np.array_equal(inl, ref["inliers"]) and info[0] >= 3
+    assert rt.tobytes() == np.ascontiguousarray(ref["Rt"], np.float64).tobytes()
+
+
 def test_ransac_trial_counts_identical(tdm, oracle, cuda):
     """Every trial's inlier count matches (read from the documented workspace
     layout: counts follow an 8-byte best word padded to 256 bytes)."""
