@@ -1,9 +1,10 @@
 """GPU parity of mutual-NN matching and RANSAC against the oracle.
 
 MNN FP32 form: indices bit-exact against the exact double-precision NN.
-MNN BF16 form (tcgen05 distance GEMM): >= 99 % index agreement.
+MNN BF16 form (tcgen05 distance GEMM): >= 99 % index agreement; near ties
+among the candidates resolved as the exact FP64 NN.
 RANSAC: identical per-trial inlier counts, winner and inlier set; the FP64
-Kabsch refit equal to the oracle's to 1e-9.
+Kabsch refit equal to the oracle's bit for bit.
 """
 import numpy as np
 import pytest
@@ -85,6 +86,45 @@ def test_mnn_bf16_agreement(tdm, oracle, cuda, n):
     ref_set = set(map(tuple, ref_pairs.tolist()))
     got_set = set(map(tuple, pairs.tolist()))
     assert len(ref_set & got_set) >= 0.99 * len(ref_set)
+
+
+def test_mnn_bf16_rescoring_near_ties(tdm, oracle, cuda):
+    """BF16 form: each of 16 queries has four near copies (an exact duplicate
+    and copies one FP32 ulp nearer / farther in one component), ~2e-7 apart
+    in squared distance -- inside the FP32 re-scoring's error interval, so
+    those queries take the FP64 pass -- and far from every other row, so all
+    four are candidates; four more queries have two exact duplicates as their
+    nearest rows.  The other queries are decided in FP32.  Every index equals
+    the exact FP64 nearest neighbour (duplicates: the lower index)."""
+    rng = np.random.default_rng(21)
+    a = rng.normal(size=(64, 512)).astype(np.float32)
+    groups = []
+    for i in range(16):
+        e = (0.02 * rng.normal(size=512)).astype(np.float32)
+        e[0] = 0.5
+        b0 = a[i] + e
+        near, far = b0.copy(), b0.copy()
+        near[0] = np.nextafter(b0[0], a[i, 0])  # one ulp towards the query
+        far[0] = np.nextafter(b0[0], np.float32(np.inf) if b0[0] > a[i, 0] else np.float32(-np.inf))
+        groups.append(np.stack([b0, b0, far, near])[rng.permutation(4)])
+    for i in range(16, 20):  # nearest rows are exact duplicates: the lower index wins
+        e = (0.02 * rng.normal(size=512)).astype(np.float32)
+        e[0] = 0.5
+        b0 = a[i] + e
+        far = b0.copy()
+        far[0] = np.nextafter(b0[0], np.float32(np.inf) if b0[0] > a[i, 0] else np.float32(-np.inf))
+        far2 = far.copy()
+        far2[0] = np.nextafter(far[0], np.float32(np.inf) if far[0] > a[i, 0] else np.float32(-np.inf))
+        groups.append(np.stack([far2, b0, far, b0]))
+    b = np.concatenate(groups + [rng.normal(size=(20, 512)).astype(np.float32)])
+    ref_pairs, ref_ab, ref_ba = oracle.mutual_nn(a, b)
+    d = ((a[:16, None, :].astype(np.float64) - b[None, :64, :].astype(np.float64)) ** 2).sum(-1)
+    assert len({round(x, 12) for x in d[0, :4]}) == 3  # duplicate, nearer, farther: three distances
+    assert all(ref_ab[i] == 4 * i + 1 for i in range(16, 20))
+    pairs, nn_ab, nn_ba = _run(tdm, cuda, a, b, "bf16")
+    assert np.array_equal(nn_ab, ref_ab) and np.array_equal(nn_ba, ref_ba)
+    assert np.array_equal(pairs, ref_pairs)
+    tdm.device_status()
 
 
 def _correspondences(rng, m, inlier_frac=0.4, noise=0.01):
