@@ -64,6 +64,7 @@ struct KParams {
   float out_qinv;
   uint8_t* out;
   int64_t out_cs;
+  uint8_t* out2;  // CTA-pair conv2 with the y-pair max: the pooled rows (out's chunk stride)
   int D, Do, nz, nyx, kgroups, cpg, cout, out_mode, relu, R, nsa, nsb, ntiles;
   int ksplit;   // K splits of a GEMM (tiles ordered m, n, split); > 1: raw FP32 partials to part
   float* part;  // [ksplit][rows][cout] when ksplit > 1
@@ -1306,6 +1307,7 @@ constexpr int kD2N = 2 * kDxfN;           // 192 accumulator columns per buffer
 constexpr int kD2Out = 2 * kDxfSub;       // 252 output rows per pair tile
 constexpr uint32_t kD2Xchg = 4u * 2u * 4u * 48u * 4u;  // [set][parity][quarter][P1 l0, P2 l0, P2 l1] x 16
 constexpr int kD2Bars = 2 * kD2NSA + 7;
+constexpr uint32_t kD2YStage = 64u * 4u * 32u;  // y-pair staging: [row / 2][set][32 B]
 constexpr int64_t kPairMaxRows = INT32_MAX - (1 << 16);  // slab rows stay below 2^31
 
 // Work units of the pair kernel: (patch b, block yb of 252 rows of a z plane,
@@ -1334,7 +1336,7 @@ __device__ __forceinline__ void epi_bar_set(int set) {
   asm volatile("bar.sync %0, 128;" ::"r"(set + 1) : "memory");
 }
 
-template <bool FP8_OUT, bool XPOOL, bool ZPOOL>
+template <bool FP8_OUT, bool XPOOL, bool ZPOOL, bool YPOOL>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_conv_dxf2_kernel(const KParams p,
                                                                                           const __grid_constant__ CUtensorMap tmA,
                                                                                           const PairSched ps) {
@@ -1345,7 +1347,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
   uint8_t* sW = smem;
   uint8_t* sA = smem + kDxfWBytes;
   float* sX = reinterpret_cast<float*>(sA + kD2NSA * a_stage);
-  float* sBias = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(sX) + kD2Xchg);  // the layer's 64 biases
+  uint4* sY = reinterpret_cast<uint4*>(reinterpret_cast<uint8_t*>(sX) + kD2Xchg);  // y-pair staging
+  float* sBias = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(sY) + kD2YStage);  // the layer's 64 biases
   int* sVote = reinterpret_cast<int*>(sBias + 64);  // [set][parity][quarter]
   uint64_t* bars = reinterpret_cast<uint64_t*>(sVote + 32);
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + kD2Bars);
@@ -1502,8 +1505,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
     // 16 channels at (set % 2) * 16 within each tap's 32
     const uint32_t col0 = (uint32_t)((set >> 1) * kDxfN + (set & 1) * 16);
     static_assert(!ZPOOL || XPOOL, "the z-pair max comes with the x-pair max");
+    static_assert(!YPOOL || ZPOOL, "the y-pair max comes with the x- and z-pair max");
     const int Do = p.Do, XO = XPOOL ? p.Do / 2 : p.Do, ZO = ZPOOL ? p.Do / 2 : p.Do;
     uint8_t* const outp = p.out + (int64_t)(n0 / (FP8_OUT ? 16 : 8)) * p.out_cs;
+    uint8_t* const outp2 = YPOOL ? p.out2 + (int64_t)(n0 / (FP8_OUT ? 16 : 8)) * p.out_cs : nullptr;
     uint32_t j = 0;
     bool stop = false;
     // z-pooled: units start on even z with an even number of tiles, and the
@@ -1518,9 +1523,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
       const int pp = w.yb * kD2Out + (int)rank * kDxfSub + L, y = pp / p.D, x = pp - y * p.D;
       const bool lane_ok = L < kDxfSub && x < Do && y < Do && (!XPOOL || (x & 1) == 0);
       const int pbase = ((w.b * ZO + (ZPOOL ? w.z0 / 2 : w.z0)) * Do + y) * XO + (XPOOL ? x / 2 : x);
+      // y-pooled: the rows of y and y + 1 (y even) at the same x are D apart;
+      // when both lie in this CTA's 126 rows they meet in shared memory and the
+      // even one stores the pooled row, otherwise (ycross) both go out x- and
+      // z-pooled and the pool pass takes their max
+      const bool ycross = YPOOL && ((y & 1) ? L < p.D : L + p.D >= kDxfSub);
+      const int fbase = YPOOL ? ((w.b * ZO + w.z0 / 2) * (Do / 2) + y / 2) * XO + x / 2 : 0;
       for (int zi = 0; zi < w.nz; ++zi) {
       const int pout = lane_ok ? pbase + (ZPOOL ? zi / 2 : zi) * Do * XO : -1;
       const bool zstore = !ZPOOL || (zi & 1);  // z-pooled: the odd tile of each z pair stores
+      const int pfin = fbase + (zi / 2) * (Do / 2) * XO;  // y-pooled output row (when pout >= 0)
       const uint32_t buf = j & 1u, use = j >> 1;
       const int got = __all_sync(0xffffffffu, wait_or_flag(accFull + 8 * buf, use & 1u, p.err, DEV_TIMEOUT_EPILOGUE) ? 1 : 0);
       int* vote = sVote + (set * 2 + (j & 1u)) * 4;
@@ -1617,8 +1629,24 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
             zkeep[0] = o;
           }
         }
-        if (zstore && pout >= 0) *reinterpret_cast<uint4*>(outp + (int64_t)pout * 16) = o;
+        if (!YPOOL && zstore && pout >= 0) *reinterpret_cast<uint4*>(outp + (int64_t)pout * 16) = o;
+        if (YPOOL && zstore) {
+          if (pout >= 0) {
+            if (ycross) *reinterpret_cast<uint4*>(outp + (int64_t)pout * 16) = o;
+            else sY[(L >> 1) * 4 + set] = o;
+          }
+          epi_bar_set(set);  // every warp of the set, every odd tile
+          if (pout >= 0 && !ycross && (y & 1) == 0) {
+            const uint4 m = sY[((L + p.D) >> 1) * 4 + set];
+            o.x = __vmaxu4(o.x, m.x);
+            o.y = __vmaxu4(o.y, m.y);
+            o.z = __vmaxu4(o.z, m.z);
+            o.w = __vmaxu4(o.w, m.w);
+            *reinterpret_cast<uint4*>(outp2 + (int64_t)pfin * 16) = o;
+          }
+        }
       } else {
+        uint4 ov[2];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           uint4 o = make_uint4(pk[(4 * h) % (FP8_OUT ? 4 : 8)], pk[(4 * h + 1) % (FP8_OUT ? 4 : 8)],
@@ -1647,7 +1675,37 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kD2Threads, 1) tc_co
               zkeep[h] = o;
             }
           }
-          if (zstore && pout >= 0) *reinterpret_cast<uint4*>(outp + h * p.out_cs + (int64_t)pout * 16) = o;
+          ov[h] = o;
+          if (!YPOOL && zstore && pout >= 0) *reinterpret_cast<uint4*>(outp + h * p.out_cs + (int64_t)pout * 16) = o;
+        }
+        if (YPOOL && zstore) {
+          // a row whose y pair shares the CTA half goes to shared memory, the
+          // others out x- and z-pooled; the even row of a pair stores the max
+          if (pout >= 0) {
+            if (ycross) {
+              *reinterpret_cast<uint4*>(outp + (int64_t)pout * 16) = ov[0];
+              *reinterpret_cast<uint4*>(outp + p.out_cs + (int64_t)pout * 16) = ov[1];
+            } else {
+              sY[((L >> 1) * 4 + set) * 2] = ov[0];
+              sY[((L >> 1) * 4 + set) * 2 + 1] = ov[1];
+            }
+          }
+          epi_bar_set(set);  // every warp of the set, every odd tile
+          if (pout >= 0 && !ycross && (y & 1) == 0) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const uint4 m = sY[(((L + p.D) >> 1) * 4 + set) * 2 + h];
+              uint32_t* wv = reinterpret_cast<uint32_t*>(&ov[h]);
+              const uint32_t* mv = reinterpret_cast<const uint32_t*>(&m);
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                __nv_bfloat162 mx = __hmax2(*reinterpret_cast<const __nv_bfloat162*>(&wv[k]),
+                                            *reinterpret_cast<const __nv_bfloat162*>(&mv[k]));
+                wv[k] = *reinterpret_cast<uint32_t*>(&mx);
+              }
+              *reinterpret_cast<uint4*>(outp2 + h * p.out_cs + (int64_t)pfin * 16) = ov[h];
+            }
+          }
         }
       }
       ++j;
@@ -1968,7 +2026,8 @@ int weight_stages(const TcLayer& L) {
 
 size_t smem_bytes(const TcLayer& L) {
   if (L.dxf && L.pair)
-    return kDxfWBytes + (size_t)kD2NSA * 16 * 8 * pair_slab_rows(L) + kD2Xchg + 256 + 128 + kSmemReserve;
+    return kDxfWBytes + (size_t)kD2NSA * 16 * 8 * pair_slab_rows(L) + kD2Xchg + kD2YStage + 256 + 128 +
+           kSmemReserve;
   if (L.dxf) return kDxfWBytes + kDxfNSA * a_stage_bytes(L) + kDxfXchg + kDxfStage + 32 + kSmemReserve;
   if (L.gather)
     return gather_stages(L) * gather_stage_bytes(L) + (L.wt ? kWtStage : 0) + (size_t)weight_stages(L) * L.nt * 128 +
@@ -2059,7 +2118,7 @@ bool gather_tile_built(int nt, int msub) {
 
 // CTA pairs of the pair form that can be resident at once on this device
 // (clusters need both CTAs on one GPC; one CTA per SM), cached per device.
-template <bool FP8_OUT, bool XPOOL, bool ZPOOL>
+template <bool FP8_OUT, bool XPOOL, bool ZPOOL, bool YPOOL>
 int dxf2_max_pairs(size_t smem) {
   static std::mutex mu;
   static std::map<int, int> cache;
@@ -2080,7 +2139,7 @@ int dxf2_max_pairs(size_t smem) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, tc_conv_dxf2_kernel<FP8_OUT, XPOOL, ZPOOL>, &cfg) != cudaSuccess || n <= 0) {
+  if (cudaOccupancyMaxActiveClusters(&n, tc_conv_dxf2_kernel<FP8_OUT, XPOOL, ZPOOL, YPOOL>, &cfg) != cudaSuccess || n <= 0) {
     cudaGetLastError();
     n = device_sm_count() / 2;
   }
@@ -2125,16 +2184,16 @@ tdm_status slab_tensor_map(const KParams& kp, CUtensorMap* map) {
   return TDM_OK;
 }
 
-template <bool FP8_OUT, bool XPOOL, bool ZPOOL>
+template <bool FP8_OUT, bool XPOOL, bool ZPOOL, bool YPOOL>
 tdm_status launch_dxf2(const KParams& kp, size_t smem, cudaStream_t s) {
-  auto kern = tc_conv_dxf2_kernel<FP8_OUT, XPOOL, ZPOOL>;
+  auto kern = tc_conv_dxf2_kernel<FP8_OUT, XPOOL, ZPOOL, YPOOL>;
   cudaError_t attr_err = raise_smem_cap(reinterpret_cast<const void*>(kern), (int)kSmemLimit);
   if (attr_err != cudaSuccess) return cuda_status(attr_err, "cudaFuncSetAttribute(tc_conv_dxf2_kernel)");
   CUtensorMap map;
   tdm_status st = slab_tensor_map(kp, &map);
   if (st) return st;
   // persistent: no more pairs than fit at once, so every pair runs from the start
-  const int max_pairs = dxf2_max_pairs<FP8_OUT, XPOOL, ZPOOL>(smem);
+  const int max_pairs = dxf2_max_pairs<FP8_OUT, XPOOL, ZPOOL, YPOOL>(smem);
   const int64_t D3 = (int64_t)kp.D * kp.D * kp.D, B = kp.rows / D3;
   PairSched ps;
   ps.nyb = (kp.Do * kp.D + kD2Out - 1) / kD2Out;
@@ -2152,6 +2211,51 @@ tdm_status launch_dxf2(const KParams& kp, size_t smem, cudaStream_t s) {
   return TDM_OK;
 }
 
+// The pool's y-pair max at the pooled positions whose two rows the CTA-pair
+// conv2 leaves in different CTA halves (a plane's rows are split into halves
+// of 126 rows: pooled y = 4, where the 9-row blocks meet, and parts of the
+// rows where a block's halves meet).  Both rows are in `in` x- and z-pooled,
+// [b][z/2][y][x/2]; their max goes to the pooled output [b][z/2][y/2][x/2],
+// whose other rows the pair kernel wrote.  E4M3 bytes of ReLU outputs order
+// like the values, so a byte-wise max is the max-pool.
+struct YCross {
+  int n;            // crossing (y/2, x/2) positions of a pooled z plane
+  uint16_t yx[64];  // y/2 << 8 | x/2
+};
+
+template <bool FP8>
+__global__ __launch_bounds__(256) void pool_ycross_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
+                                                          int64_t cs, int nchunks, int64_t planes, int Do,
+                                                          const YCross c) {
+  const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  const int64_t per = (int64_t)c.n * nchunks;
+  if (i >= planes * per) return;
+  const int64_t bz = i / per;  // b * Do/2 + z/2
+  const int r = (int)(i - bz * per), j = r / c.n, e = r - j * c.n;
+  const int yp = c.yx[e] >> 8, xp = c.yx[e] & 0xff, Dh = Do / 2;
+  const uint8_t* src = in + (int64_t)j * cs;
+  const uint4 a = __ldg(reinterpret_cast<const uint4*>(src + ((bz * Do + 2 * yp) * Dh + xp) * 16));
+  const uint4 b = __ldg(reinterpret_cast<const uint4*>(src + ((bz * Do + 2 * yp + 1) * Dh + xp) * 16));
+  uint4 o;
+  if (FP8) {
+    o.x = __vmaxu4(a.x, b.x);
+    o.y = __vmaxu4(a.y, b.y);
+    o.z = __vmaxu4(a.z, b.z);
+    o.w = __vmaxu4(a.w, b.w);
+  } else {
+    const uint32_t* av = reinterpret_cast<const uint32_t*>(&a);
+    const uint32_t* bv = reinterpret_cast<const uint32_t*>(&b);
+    uint32_t* ov = reinterpret_cast<uint32_t*>(&o);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      __nv_bfloat162 m = __hmax2(*reinterpret_cast<const __nv_bfloat162*>(&av[k]),
+                                 *reinterpret_cast<const __nv_bfloat162*>(&bv[k]));
+      ov[k] = *reinterpret_cast<uint32_t*>(&m);
+    }
+  }
+  *reinterpret_cast<uint4*>(out + (int64_t)j * cs + ((bz * Dh + yp) * Dh + xp) * 16) = o;
+}
+
 template <int MSUB, bool FP8_OUT, bool XPOOL>
 tdm_status launch_dxf(const KParams& kp, size_t smem, cudaStream_t s) {
   auto kern = tc_conv_dxf_kernel<MSUB, FP8_OUT, XPOOL>;
@@ -2166,6 +2270,30 @@ tdm_status launch_dxf(const KParams& kp, size_t smem, cudaStream_t s) {
 }
 
 }  // namespace
+
+tdm_status launch_pool_ycross(const TcLayer& L, const uint8_t* in, int64_t cs, int B, uint8_t* out, cudaStream_t s) {
+  TDM_REQUIRE(L.dxf && L.pair && L.Do % 2 == 0 && L.Do / 2 < 256, "pool: the y-pair finish follows the CTA-pair conv2");
+  TDM_REQUIRE(in && out && (cs & 15) == 0 && B >= 0, "pool: bad arguments");
+  YCross c{};
+  const int Dh = L.Do / 2;
+  for (int yp = 0; yp < Dh; ++yp)
+    for (int xp = 0; xp < Dh; ++xp) {
+      const int pp = 2 * yp * L.D + 2 * xp;  // the even row's index in its z plane; its partner is pp + D
+      if (pp / kDxfSub != (pp + L.D) / kDxfSub) {
+        TDM_REQUIRE(c.n < 64, "pool: too many crossing y pairs");
+        c.yx[c.n++] = (uint16_t)(yp << 8 | xp);
+      }
+    }
+  if (B == 0 || c.n == 0) return TDM_OK;
+  const int nchunks = L.fp8_out ? 4 : 8;
+  const int64_t planes = (int64_t)B * Dh, n = planes * c.n * nchunks;
+  if (L.fp8_out)
+    pool_ycross_kernel<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, cs, nchunks, planes, L.Do, c);
+  else
+    pool_ycross_kernel<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, cs, nchunks, planes, L.Do, c);
+  TDM_CHECK_LAUNCH("pool_ycross_kernel");
+  return TDM_OK;
+}
 
 // conv1 of B patches into conv2's chunk-planar BF16 input (out_cs bytes
 // between its 8 chunks); weights packed as the conv1 GEMM layer's.
@@ -2250,6 +2378,7 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   kp.out_qinv = a.out_qinv;
   kp.out = a.out;
   kp.out_cs = a.out_cs;
+  kp.out2 = a.out2;
   kp.D = L.D;
   kp.Do = L.Do;
   kp.nz = L.nz;
@@ -2265,7 +2394,7 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
   if (L.dxf && L.pair && !tc_pair_form_applies(L, a.rows)) {
     // slab rows are 32-bit tensor coordinates and units are whole patches:
     // other inputs take the single-CTA form (same bits)
-    TDM_REQUIRE(!a.zpool, "tc layer: the z-pair max needs the CTA-pair form");
+    TDM_REQUIRE(!a.zpool && !a.out2, "tc layer: the z- and y-pair max need the CTA-pair form");
     TcLayer L1 = L;
     L1.pair = false;
     return launch_tc_layer(L1, a, s);
@@ -2284,12 +2413,18 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s) {
     kp.total_tiles = (a.rows + kD2Out - 1) / kD2Out;
     const size_t smem = smem_bytes(L);
     TDM_REQUIRE(!a.zpool || (a.xpool && L.Do % 2 == 0), "tc layer: a z-pooled output needs the x-pooled form, even Do");
+    TDM_REQUIRE(!a.out2 || (a.zpool && (reinterpret_cast<uintptr_t>(a.out2) & 15) == 0),
+                "tc layer: the y-pooled output needs the z-pooled form and 16-byte alignment");
     if (L.fp8_out) {
-      if (a.zpool) return launch_dxf2<true, true, true>(kp, smem, s);
-      return a.xpool ? launch_dxf2<true, true, false>(kp, smem, s) : launch_dxf2<true, false, false>(kp, smem, s);
+      if (a.zpool)
+        return a.out2 ? launch_dxf2<true, true, true, true>(kp, smem, s) : launch_dxf2<true, true, true, false>(kp, smem, s);
+      return a.xpool ? launch_dxf2<true, true, false, false>(kp, smem, s)
+                     : launch_dxf2<true, false, false, false>(kp, smem, s);
     }
-    if (a.zpool) return launch_dxf2<false, true, true>(kp, smem, s);
-    return a.xpool ? launch_dxf2<false, true, false>(kp, smem, s) : launch_dxf2<false, false, false>(kp, smem, s);
+    if (a.zpool)
+      return a.out2 ? launch_dxf2<false, true, true, true>(kp, smem, s) : launch_dxf2<false, true, true, false>(kp, smem, s);
+    return a.xpool ? launch_dxf2<false, true, false, false>(kp, smem, s)
+                   : launch_dxf2<false, false, false, false>(kp, smem, s);
   }
   if (L.dxf) {
     TDM_REQUIRE(tc_layer_fits(L), "tc layer: unsupported dx-fused tile");

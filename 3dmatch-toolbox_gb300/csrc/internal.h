@@ -84,6 +84,10 @@ struct TcArgs {
   float out_qinv;  // FP8 output: 1/scale used to quantise
   bool xpool = false;  // dx-fused conv2: write the max of each x pair (x extent Do/2)
   bool zpool = false;  // with xpool, CTA-pair form only: also the max of each z pair (z extent Do/2)
+  // with zpool: the pooled rows ([b][z/2][y/2][x/2], out_cs between chunks) of
+  // the y pairs whose rows share a CTA half go here; `out` keeps the x- and
+  // z-pooled rows of the others, which launch_pool_ycross finishes
+  uint8_t* out2 = nullptr;
   float* part = nullptr;  // split-K partial sums, [ksplit][rows][cout] FP32
 };
 
@@ -93,6 +97,9 @@ tdm_status launch_tc_layer(const TcLayer& L, const TcArgs& a, cudaStream_t s);
 // Whether launch_tc_layer runs layer L over `rows` input rows in the CTA-pair
 // form (which alone can take the z-pair max, TcArgs::zpool).
 bool tc_pair_form_applies(const TcLayer& L, int64_t rows);
+// The y-pair max of the pooled positions the CTA-pair conv2 (layer L, y-pooled
+// into `out`) left to a pool pass: reads its x- and z-pooled rows in `in`.
+tdm_status launch_pool_ycross(const TcLayer& L, const uint8_t* in, int64_t cs, int B, uint8_t* out, cudaStream_t s);
 // conv1 with its im2col operand built in shared memory (L = the conv1 GEMM
 // layer's packed weights and bias); writes conv2's chunk-planar BF16 input.
 tdm_status launch_conv1_tc(const float* patches, int B, const TcLayer& L, uint8_t* out, int64_t out_cs,

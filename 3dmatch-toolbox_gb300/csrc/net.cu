@@ -391,7 +391,10 @@ Bf16Plan bf16_plan(const tdm_net* net, int B) {
   auto chunks = [](int l) { return kCin[l] / 8; };
   size_t b0 = 0, b1 = 0;
   for (int l : {1, 2, 4, 6, 8}) b0 = std::max(b0, (size_t)(l == 7 ? 1728 : chunks(l)) * P.rows_alloc[l] * 16);
-  b1 = std::max(b1, (size_t)8 * ((int64_t)B * 17576 + 8) * 16);  // conv2 output (pre-pool)
+  // conv2 output (pre-pool, 26^3 rows per chunk); the CTA-pair form uses the
+  // first quarter for x- and z-pooled rows and writes conv3's pooled input
+  // (plus conv3's tail rows) after them
+  b1 = std::max(b1, (size_t)8 * ((int64_t)B * 17576 + 8) * 16);
   for (int l : {3, 5}) b1 = std::max(b1, (size_t)chunks(l) * P.rows_alloc[l] * 16);
   b1 = std::max(b1, (size_t)1728 * P.rows_alloc[7] * 16);  // conv7 -> conv8 flattened operand
   P.off1 = round16((int64_t)b0) + 4096;
@@ -460,8 +463,16 @@ tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, in
       a.out_cs = out_cs;
       // the epilogue takes the pool's x-pair max unless conv2's own response is wanted
       a.xpool = stop != 1 && L.dxf;
-      // the CTA-pair form also takes the z-pair max (z extent 13)
+      // the CTA-pair form also takes the z-pair max (z extent 13) and, for y
+      // pairs within one CTA, the y-pair max: the pooled rows (conv3's input)
+      // go after the x- and z-pooled ones in conv2's output buffer, which is
+      // sized for the unpooled 26^3 rows (conv2 still reads buffer 0 while it
+      // writes them)
       a.zpool = a.xpool && tc_pair_form_applies(L, a.rows);
+      if (a.zpool) {
+        const int64_t xz_rows = ((int64_t)B * 13 * 26 * 13 + 15) / 16 * 16;
+        a.out2 = dst + xz_rows * 16;
+      }
     } else {
       out_cs = P.rows_alloc[l + 1] * 16;
       a.out = dst;
@@ -476,6 +487,19 @@ tdm_status forward_tc(tdm_net* net, const float* patches, int B, float* desc, in
       const bool taps = L.out_mode == TC_OUT_C8_TAPS;
       if (L.fp8_out) return c16_response(dst, out_cs, B, l, taps, net->act_scale[l + 1], desc, s);
       return c8_response(dst, out_cs, B, l, taps, desc, s);
+    }
+    if (l == 1 && a.out2) {  // finish the y pairs that crossed CTA halves; conv3 reads a.out2
+      ev = net->begin(9, s);
+      st = launch_pool_ycross(L, dst, out_cs, B, a.out2, s);
+      net->end(ev, s);
+      if (st) return st;
+      if (stop == kPool) {
+        if (fp8) return c16_response(a.out2, out_cs, B, kPool, false, net->act_scale[2], desc, s);
+        return c8_response(a.out2, out_cs, B, kPool, false, desc, s);
+      }
+      cur = a.out2;
+      cur_cs = out_cs;
+      continue;
     }
     if (l == 1) {  // pool 26^3 -> 13^3 back into buffer 0 as conv3's input
       int64_t pcs = P.rows_alloc[2] * 16;
