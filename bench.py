@@ -472,7 +472,7 @@ def run_ours(args, rank, world, local):
         # burst peak: conv2 runs inside a ~14 ms step at full clocks, not a
         # seconds-long loop under the power cap
         peak = peaks["bf16_tflops"] if prec == "bf16" else None
-        roof = {"kernel": "tc_conv_dxf2_kernel<bf16,x-pooled,z-pooled> (conv2 on CTA pairs, %d patches per launch)" % (2 * k),
+        roof = {"kernel": "tc_conv_dxf2_kernel<bf16,x-,z-,y-pooled> (conv2 on CTA pairs, %d patches per launch)" % (2 * k),
                 "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if peak else None, "peak_source": peak_kind + " bf16 burst",
                 "traffic": profile_traffic("conv2_pair_bf16"),
