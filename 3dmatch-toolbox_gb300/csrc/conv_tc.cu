@@ -1274,25 +1274,29 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_dxf_kernel(const KParams 
 // halves above (the leader's 110.6 KB give channels 0..31, the peer's
 // 32..63).  Each SM still reads 7 KB per MMA, now for 96 cycles of math.
 //
-// A pair tile is 252 output rows: the leader computes MMA rows [m0, m0 + 128)
-// and stores outputs [m0, m0 + 126), the peer [m0 + 126, ...).  Roles:
-//   warp 0, lane 0 (both CTAs): weights once, then its own A slabs (three dz
-//     stages per tile) by bulk copies on its own barriers;
+// A pair tile is 252 output rows of one z plane: the leader computes MMA rows
+// [m0, m0 + 128) and stores outputs [m0, m0 + 126), the peer [m0 + 126, ...).
+// Work units walk z through a column of such plane blocks, so consecutive
+// tiles share two of their three z slabs (PairSched / pair_unit below).
+// Roles:
+//   warp 0, lane 0 (both CTAs): weights once, then its own half of each slab
+//     by a tiled tensor copy (.cta_group::2) that completes on the leader's
+//     barrier, one slab per tile;
 //   warp 1, lane 0: the leader issues every MMA and commits with multicast to
 //     both CTAs' barriers (stage free, accumulator full); the peer relays its
-//     own "weights landed" and "slab landed" completions to the leader by
-//     remote mbarrier arrives;
-//   warps 2-9 (both CTAs): two epilogue sets, set h draining the 96 columns of
-//     channel half h for the CTA's 128 TMEM lanes (the dx row-shift sum of the
-//     kernel above); each warp signals the leader's accumulator-empty barrier
-//     (eight local and eight remote arrivals, the remote ones relaxed: a
-//     release at cluster scope held the warp ~1,000 cycles) as soon as its
-//     accumulator reads are done, then adds, packs, takes the x-pair max and
-//     stores each lane's 16-byte chunks straight to global memory (a warp's
-//     even lanes write consecutive pooled rows).  Staging the tile in shared
-//     memory for bulk stores cost the warp issuing them ~2,500 cycles a tile
-//     (two dozen small copies behind the slab loads in the copy engine) and a
-//     second barrier.
+//     "weights landed" completion to the leader by a remote mbarrier arrive;
+//   warps 2-17 (both CTAs): four epilogue sets of 16 output channels x four
+//     TMEM lane quarters.  A warp reads its 48 accumulator columns (the three
+//     dx taps of its channels), signals the leader's accumulator-empty barrier
+//     at once (local, or a relaxed remote arrive: a release at cluster scope
+//     held the warp ~1,000 cycles), then adds the row-shifted taps (lane
+//     shuffles; the quarter boundary through shared memory), packs, and takes
+//     the pool's x-pair max (lane L ^ 1), z-pair max (tiles z and z + 1 of a
+//     unit go through the same warp) and, for y pairs within the CTA's rows,
+//     the y-pair max (shared memory, one set barrier per odd tile), storing
+//     each lane's 16-byte chunks straight to global memory.  Staging whole
+//     tiles in shared memory for bulk stores cost the warp issuing them ~2,500
+//     cycles a tile.
 // TMEM: one pair allocation (issued together by warp 1 of both CTAs), two
 // accumulator buffers of 192 columns.  Every mbarrier wait is bounded; both
 // CTAs always reach the cluster barriers (no early exit), so a timeout in one
