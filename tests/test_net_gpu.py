@@ -299,16 +299,19 @@ def test_fresh_nets_on_nonblocking_streams(tdm, weights, patches, precision):
 
 
 @pytest.mark.parametrize("precision", ["bf16", "fp8"])
-def test_fused_x_pool_same_bits(tdm, weights, patches, precision):
-    """conv2's epilogue takes the pool's x-pair max; pool1 equals the 2x2x2 max of
-    the unfused conv2 response bit for bit (max commutes with the rounding)."""
+@pytest.mark.parametrize("nb", [1, 3, 6])
+def test_fused_x_pool_same_bits(tdm, weights, patches, precision, nb):
+    """conv2's epilogue takes the pool's x-, z- and (within a CTA half) y-pair
+    max, and a small pass the y pairs that cross halves; pool1 equals the
+    2x2x2 max of the unfused conv2 response bit for bit (max commutes with the
+    rounding).  One patch splits the z walk into short units."""
     net = tdm.Net(weights, precision=precision)
     if precision == "fp8":
         net.calibrate(patches)
-    b = patches[:6].contiguous()
+    b = patches[:nb].contiguous()
     c2 = net.response("conv2", b).cpu().numpy()   # [b, 26, 26, 26, 64], unfused epilogue
-    p1 = net.response("pool1", b).cpu().numpy()   # [b, 13, 13, 13, 64], fused x-pair max
-    want = c2.reshape(6, 13, 2, 13, 2, 13, 2, 64).max(axis=(2, 4, 6))
+    p1 = net.response("pool1", b).cpu().numpy()   # [b, 13, 13, 13, 64], fused pair maxima
+    want = c2.reshape(nb, 13, 2, 13, 2, 13, 2, 64).max(axis=(2, 4, 6))
     assert np.array_equal(p1, want)
     tdm.device_status()
 
