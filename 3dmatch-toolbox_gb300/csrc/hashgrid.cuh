@@ -103,11 +103,12 @@ __global__ void insert_kernel(const float* __restrict__ p, int n, float cell, fl
 }
 
 // Exclusive scan of the slot counts: per-block scan, block totals, add.
-__global__ void scan_block_kernel(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ out,
-                                  int32_t* __restrict__ sums) {
+// `out` may be `in` (each thread reads its element once, before writing it).
+__global__ void scan_block_kernel(const int32_t* in, int64_t n, int32_t* out, int32_t* __restrict__ sums) {
   __shared__ int32_t s[kScanBlock];
   const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
-  s[threadIdx.x] = i < n ? in[i] : 0;
+  const int32_t mine = i < n ? in[i] : 0;
+  s[threadIdx.x] = mine;
   __syncthreads();
   for (int o = 1; o < kScanBlock; o <<= 1) {
     const int32_t v = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
@@ -115,7 +116,7 @@ __global__ void scan_block_kernel(const int32_t* __restrict__ in, int64_t n, int
     s[threadIdx.x] += v;
     __syncthreads();
   }
-  if (i < n) out[i] = s[threadIdx.x] - (i < n ? in[i] : 0);
+  if (i < n) out[i] = s[threadIdx.x] - mine;
   if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = s[threadIdx.x];
 }
 
