@@ -2152,7 +2152,7 @@ int dxf2_max_pairs(size_t smem) {
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
-// against the driver library).
+// against libcuda).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
