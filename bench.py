@@ -922,6 +922,7 @@ def run_registration(args, rank, world, local):
                         match_precision="bf16", ransac_seed=20260000, ransac_iters=args.ransac_iters)
     pairs = [(i, j) for i in range(F) for j in range(i + 1, F)]
     pipe.register(pts[0], pts[1], seed=1, k=args.keypoints)  # warm-up
+    tdm.overlap(pts[0], pts[1], np.eye(4)[:3], 0.05)  # warm-up: the first call in a process takes ~0.24 s
     # describe once, register many (getKeyptsAndDesc.m, then register2Fragments.m
     # per pair): every view is described into the device store once
     store = tdm.Store(F * 2100 * args.keypoints + (1 << 20))
